@@ -1,0 +1,345 @@
+"""Benchmark: ms to relative residual 1e-10 on the 2D 1024^2 random-coefficient problem.
+
+One step = one complete solve (coefficient hierarchy + cycles until
+||rhs - L_h phi||_2 / ||rhs||_2 <= 1e-10) of the seeded synthetic problem
+``jsolver_gb300.workloads.random_2d(1024, seed)``: D_xx, D_yy = exp(GRF sigma 1, corr.
+length 0.05), lambda ~ U[0, 10], rhs = L_h sin(pi x) sin(2 pi y).
+
+Our arm (default): ``value`` is the device time of a solve with inputs resident in HBM,
+through the C ABI (jmg_solve), timed with CUDA events on the solving stream; L2 is
+flushed (256 MB write) before every timed solve. ``e2e`` is the same solve through the
+public API (solve_2d on CUDA tensors) with the host->device copies of the inputs from
+pinned memory and the device->host copy of phi and the count inside the timed region.
+``--gpus N`` under torchrun runs N independent replicas (the path does not shard).
+
+Reference arm (``--impl reference``): the reference's CPU path cannot run here (JAX is
+absent), so the oracle's C/OpenMP restatement of it is timed on the host cores, full
+solves, same workload and metric.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms to rel. residual 1e-10 (2D 1024^2 random-coefficient problem)"
+RTOL = 1e-10
+M = 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--cycle", default="V", choices=["V", "W", "F"])
+    ap.add_argument("--m", type=int, default=M)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def cycle_kw(c):
+    return {"V": {}, "W": {"gamma": 2}, "F": {"fcycle": True}}[c]
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                self.out = ""
+        return False
+
+    def summary(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in getattr(self, "out", "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from jsolver_gb300 import workloads
+    from oracle import c_oracle
+    from oracle.grid import OracleGrid1D
+    p = workloads.random_2d(args.m, seed=args.seed)
+    g = OracleGrid1D(args.m)
+    nthreads = os.cpu_count() or 1
+    times, counts = [], []
+    kw = cycle_kw(args.cycle)
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        phi, cnt, rr = c_oracle.solve((g, g), p["phi0"], p["rhs"], p["lam"], (p["D_xx"], p["D_yy"]), stop="residual",
+                                      rtol=RTOL, nthreads=nthreads, **kw)
+        dt = (time.perf_counter() - t0) * 1e3
+        if it >= args.warmup:
+            times.append(dt)
+            counts.append(cnt)
+    ms = float(np.median(times))
+    line = {
+        "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded GRF coefficients, manufactured rhs)",
+        "impl": "reference",
+        "config": {"workload": f"2d-{args.m}x{args.m}-random-coeff (arrays {args.m + 3}^2 float64)",
+                   "cycle": args.cycle, "stop": f"rel. residual <= {RTOL}", "cycles": counts[-1]},
+        "cpu_baseline": {"value": ms, "unit": "ms", "cores": nthreads, "kind": "port",
+                         "sample": f"{args.steps} full solves (median), C/OpenMP restatement of the reference "
+                                   f"algorithm (oracle/jmg_oracle.c), {nthreads} threads; the reference's own JAX "
+                                   "path cannot run without JAX"},
+        "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "final_rel_residual": rr,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(p, m, cycles_needed, kw, budget_s=20.0):
+    """Time the C oracle on the host cores: a bounded number of cycles, scaled to a solve."""
+    from oracle import c_oracle
+    from oracle.grid import OracleGrid1D
+    g = OracleGrid1D(m)
+    nthreads = os.cpu_count() or 1
+    args = ((g, g), p["phi0"], p["rhs"], p["lam"], (p["D_xx"], p["D_yy"]))
+    t0 = time.perf_counter()
+    c_oracle.solve(*args, fixed=True, max_iters_outer=1, nthreads=nthreads, **kw)
+    t1 = time.perf_counter() - t0
+    n2 = int(max(2, min(cycles_needed, (budget_s - t1) / max(t1 * 0.8, 1e-3))))
+    t0 = time.perf_counter()
+    c_oracle.solve(*args, fixed=True, max_iters_outer=n2, nthreads=nthreads, **kw)
+    t2 = time.perf_counter() - t0
+    per_cycle = max((t2 - t1) / (n2 - 1), 1e-9)
+    setup = max(t1 - per_cycle, 0.0)
+    est = (setup + per_cycle * cycles_needed) * 1e3
+    return {"value": est, "unit": "ms", "cores": nthreads, "kind": "port",
+            "sample": f"C/OpenMP restatement (oracle/jmg_oracle.c): 1 and {n2} fixed cycles timed at full size "
+                      f"({setup * 1e3:.0f} ms set-up + {per_cycle * 1e3:.1f} ms/cycle), scaled to the "
+                      f"{cycles_needed} cycles a solve to 1e-10 takes"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    import torch
+    import torch.distributed as dist
+    ws_n, rank, local = dist_env()
+    if ws_n > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from jsolver_gb300 import _engine, _lib, workloads
+    from jsolver_gb300.grid_1d import grid_1D
+    from jsolver_gb300.solver_2d import solve_2d
+
+    m = args.m
+    p = workloads.random_2d(m, seed=args.seed + rank)
+    g = grid_1D(m)
+    kw = cycle_kw(args.cycle)
+    opts = dict(stop="residual", rtol=RTOL, precision=args.form, **kw)
+    lib = _lib.load()
+    cfg = _engine.make_config(**opts)
+    plan = _lib.Plan(_engine.make_grid((g, g)), cfg)
+    stream = torch.cuda.Stream(dev)
+    d = {k: torch.from_numpy(p[k]).to(dev) for k in ("phi0", "rhs", "lam", "D_xx", "D_yy")}
+    out = torch.empty_like(d["phi0"])
+    count = torch.zeros((), dtype=torch.int64, device=dev)
+    wsb = torch.empty(plan.workspace_bytes, dtype=torch.uint8, device=dev)
+    coeffs = _lib.JmgCoeffs()
+    coeffs.lam = d["lam"].data_ptr()
+    coeffs.D[0] = d["D_xx"].data_ptr()
+    coeffs.D[1] = d["D_yy"].data_ptr()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    vp = ctypes.c_void_p
+
+    def solve_dev(s):
+        _lib.check(lib.jmg_solve(plan.handle, vp(d["phi0"].data_ptr()), vp(d["rhs"].data_ptr()), ctypes.byref(coeffs),
+                                 vp(out.data_ptr()), vp(count.data_ptr()), vp(wsb.data_ptr()),
+                                 ctypes.c_size_t(wsb.numel()), vp(s.cuda_stream)))
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            solve_dev(stream)
+        stream.synchronize()
+        cycles = int(count.item())
+        # timed region
+        if ws_n > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        evs = []
+        with Clocks(local) as clk:
+            for _ in range(args.steps):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                solve_dev(stream)
+                e1.record(stream)
+                evs.append((e0, e1))
+            torch.cuda.synchronize()
+        if ws_n > 1:
+            dist.barrier()
+        times = [a.elapsed_time(b) for a, b in evs]
+        ms = float(np.mean(times))
+        if ws_n > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        cycles = int(count.item())
+        # relative residual of the result, FP64 on the device
+        rr_t = torch.empty((), dtype=torch.float64, device=dev)
+        _lib.check(lib.jmg_rel_residual(plan.handle, vp(out.data_ptr()), vp(d["rhs"].data_ptr()), vp(rr_t.data_ptr()),
+                                        vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()), vp(stream.cuda_stream)))
+        stream.synchronize()
+        rel_res = float(rr_t.item())
+        err_exact = float(np.abs(out.cpu().numpy() - p["phi_exact"]).max())
+
+        # dominant kernel: fine-level red-black sweep, timed alone (2 colour launches/sweep)
+        nsw = 50
+        _lib.check(lib.jmg_op_smooth_ws(plan.handle, 0, 5, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()),
+                                        vp(stream.cuda_stream)))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush.zero_()
+        e0.record(stream)
+        _lib.check(lib.jmg_op_smooth_ws(plan.handle, 0, nsw, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()),
+                                        vp(stream.cuda_stream)))
+        e1.record(stream)
+        stream.synchronize()
+        sweep_ms = e0.elapsed_time(e1) / nsw
+        n0 = (m + 3) ** 2
+        s_bytes = 8 if args.form == "fp64" else 4
+        alg_bytes_sweep = (2 + 4) * 8 * n0  # (d+4)*s*N0, d = 2, FP64 fine-level smoother
+        launch_ms = sweep_ms / 2
+        achieved = alg_bytes_sweep / 2 / (launch_ms * 1e-3) / 1e9
+
+        # end to end through the public API from pinned host buffers
+        host = {k: torch.from_numpy(p[k]).pin_memory() for k in ("phi0", "rhs", "lam", "D_xx", "D_yy")}
+        dst = {k: torch.empty_like(d[k]) for k in host}
+        phi_host = torch.empty(out.shape, dtype=torch.float64).pin_memory()
+        cnt_host = torch.empty((), dtype=torch.int64).pin_memory()
+
+        def e2e_step():
+            for k in host:
+                dst[k].copy_(host[k], non_blocking=True)
+            phi, cnt = solve_2d(g, g, dst["phi0"], dst["rhs"], dst["lam"], dst["D_xx"], dst["D_yy"], **opts)
+            phi_host.copy_(phi, non_blocking=True)
+            cnt_host.copy_(cnt, non_blocking=True)
+
+        for _ in range(2):
+            e2e_step()
+        stream.synchronize()
+        e2e_t = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            e2e_step()
+            e1.record(stream)
+            e1.synchronize()
+            e2e_t.append(e0.elapsed_time(e1))
+        e2e_ms = float(np.mean(e2e_t))
+        h2d = sum(t.numel() * 8 for t in host.values())
+        d2h = phi_host.numel() * 8 + 8
+
+    fixed_n, per_cycle = ctypes.c_int64(), ctypes.c_int64()
+    lib.jmg_plan_launch_counts(plan.handle, ctypes.byref(fixed_n), ctypes.byref(per_cycle))
+    launches = args.steps * (fixed_n.value + per_cycle.value * cycles)
+
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            traffic = json.load(f).get("k_sweep_color2d_fp64_1024")
+    except (OSError, ValueError):
+        pass
+
+    line = {
+        "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": ws_n, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.form == "fp64" else "f32+f64",
+        "data": "synthetic (seeded GRF coefficients, manufactured rhs; no dataset in the reference)",
+        "config": {"workload": f"2d-{m}x{m}-random-coeff (arrays {m + 3}^2 float64)", "cycle": args.cycle,
+                   "form": args.form, "stop": f"rel. residual <= {RTOL}", "cycles": cycles,
+                   "l2": "flushed (256 MB write) before every timed solve", "parallelism": f"replicas x{ws_n}"},
+        "solves_per_s": 1e3 / ms * ws_n,
+        "final_rel_residual": rel_res,
+        "max_err_vs_exact_discrete": err_exact,
+        "roofline": {"bound": "hbm", "kernel": "k_sweep_color2d<double> (fine level, one colour)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_src,
+                     "alg_bytes_per_launch": alg_bytes_sweep / 2, "launch_ms": launch_ms,
+                     "traffic": traffic},
+        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+    }
+    line["clocks"] = clk.summary()
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(p, m, cycles, kw)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws_n > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

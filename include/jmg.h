@@ -1,0 +1,169 @@
+/*
+ * jmg.h — C ABI of the GB300 geometric-multigrid solver (jsolver_gb300).
+ *
+ * Drop-in boundary for davef96/jsolver's solve path. The reference's public entry
+ * points are the jit-compiled functions
+ *     solve_2d(grid_x, grid_y, phi, rhs, lam, D_xx, D_yy, *, D_xy, fixed, epsilon,
+ *              gamma, fcycle, skip_pre, nu1, nu2, max_iters_outer, max_iters_inner)
+ *         -> (phi, count)                                   jsolver/solver_2d.py:196-236
+ *     solve_3d(grid_x, grid_y, grid_z, phi, rhs, lam, D_xx, D_yy, D_zz, *, fixed, ...)
+ *                                                           jsolver/solver_3d.py:196-237
+ * and the Solver_2D / Solver_3D methods below them (solver_2d.py:238-692,
+ * solver_3d.py:239-706). Each declaration below names the reference interface it
+ * replaces.
+ *
+ * Conventions
+ *  - All arrays are float64 device pointers in the reference's padded layout: 2D
+ *    row-major [y][x] of shape (my+3, mx+3); 3D [z][y][x] of shape (mz+3, my+3, mx+3)
+ *    (solver_3d.py:210-212). A NULL coefficient pointer selects the scalar argument
+ *    next to it (the reference's "scalar lam / scalar D" forms).
+ *  - The caller owns every buffer, including the workspace. A JmgPlan is a host
+ *    object created and destroyed by the caller; it caches the captured CUDA graph of
+ *    the cycle loop for the pointers it was last run with.
+ *  - Every call is asynchronous on the given stream and returns a status code
+ *    (JMG_OK or a JMG_ERR_*); nothing throws across the ABI. jmg_last_error() gives
+ *    the message of the last failure on the calling thread. Validation errors carry
+ *    the reference's ValueError messages (solver_2d.py:292-321, 449-453).
+ *  - Dynamic mode needs no host synchronisation: the cycle count is written to the
+ *    device int64 pointed to by count_out.
+ */
+#ifndef JMG_H
+#define JMG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* jmg_stream_t; /* same type as cudaStream_t */
+
+enum {
+  JMG_OK = 0,
+  JMG_ERR_VALUE = 1,     /* invalid argument: the reference raises ValueError */
+  JMG_ERR_CUDA = 2,      /* a CUDA runtime call failed */
+  JMG_ERR_WORKSPACE = 3  /* workspace missing or too small */
+};
+
+enum { JMG_STOP_DISTANCE = 0, JMG_STOP_RESIDUAL = 1 };
+enum { JMG_PREC_FP64 = 0, JMG_PREC_MIXED = 1 };
+
+/* Geometry: the fields of grid_1D the solver reads (jsolver/grid_1d.py:82-114). */
+typedef struct JmgGrid {
+  int32_t ndim;         /* 2 or 3 */
+  int32_t m[3];         /* resolution per axis x, y, z (grid_1D.mx); z unused in 2D */
+  double idel[3];       /* 1/h per axis (grid_1D.idel) */
+  int32_t is_linear[3]; /* grid_1D.is_linear */
+} JmgGrid;
+
+/* Solver configuration: the static arguments of solve_2d/solve_3d (solver_2d.py:197),
+ * plus the stopping rule and precision of this library's extensions. */
+typedef struct JmgConfig {
+  int32_t fixed;           /* 1: exactly max_iters_outer cycles (fori_loop, solver_2d.py:461-463) */
+  int32_t gamma;           /* recursive calls per level: 1 = V, 2 = W */
+  int32_t fcycle;          /* F-cycle (solver_2d.py:609-610) */
+  int32_t skip_pre;        /* pre-smooth once before the loop, not per cycle at level 0 */
+  int32_t nu1, nu2;        /* pre-/post-smoothing sweeps */
+  int64_t max_iters_outer; /* cycle limit (count in fixed mode) */
+  int64_t max_iters_inner; /* accepted for API parity; unused, as in the reference */
+  double epsilon;          /* distance threshold of the dynamic loop (solver_2d.py:465-467) */
+  int32_t stop;            /* JMG_STOP_DISTANCE (reference) or JMG_STOP_RESIDUAL */
+  double rtol;             /* relative-residual target for JMG_STOP_RESIDUAL */
+  int32_t precision;       /* JMG_PREC_FP64 or JMG_PREC_MIXED (FP32 cycles, FP64 refinement) */
+  int32_t inner_cycles;    /* FP32 cycles per refinement step (JMG_PREC_MIXED) */
+} JmgConfig;
+
+/* Coefficients of one solve: lam, D_xx, D_yy (, D_zz) and optional D_xy. */
+typedef struct JmgCoeffs {
+  const double* lam; double lam_scalar;
+  const double* D[3]; double D_scalar[3]; /* D_xx, D_yy, D_zz */
+  const double* D_xy;                     /* 2D off-diagonal component or NULL */
+} JmgCoeffs;
+
+typedef struct JmgPlan JmgPlan;
+
+/* Fills cfg with the reference defaults (solver_2d.py:197): dynamic, epsilon 1e-12,
+ * gamma 1, no F-cycle, no skip_pre, nu1 = nu2 = 1, max_iters = int32 max. */
+void jmg_config_default(JmgConfig* cfg);
+
+/* Validates grid and configuration and lays out the level hierarchy
+ * (Solver_2D.__init__ / compute_shapes / compute_idel, solver_2d.py:247-324;
+ * solver_3d.py:248-336). Raises the reference's messages as JMG_ERR_VALUE. */
+int jmg_plan_create(JmgPlan** plan, const JmgGrid* grid, const JmgConfig* cfg);
+int jmg_plan_destroy(JmgPlan* plan);
+size_t jmg_plan_workspace_bytes(const JmgPlan* plan);
+int jmg_plan_levels(const JmgPlan* plan);
+
+/* Full solve (Solver_2D.solve / Solver_3D.solve, solver_2d.py:423-479,
+ * solver_3d.py:431-486). phi0 and phi_out may alias. count_out: device int64. */
+int jmg_solve(JmgPlan* plan, const double* phi0, const double* rhs, const JmgCoeffs* coeffs,
+              double* phi_out, int64_t* count_out, void* workspace, size_t workspace_bytes,
+              jmg_stream_t stream);
+
+/* One-shot form of jmg_solve for 2D / 3D (creates and destroys a plan). */
+int jmg_solve2d_f64(const JmgGrid* grid, const JmgConfig* cfg, const double* phi0,
+                    const double* rhs, const JmgCoeffs* coeffs, double* phi_out,
+                    int64_t* count_out, void* workspace, size_t workspace_bytes,
+                    jmg_stream_t stream);
+int jmg_solve3d_f64(const JmgGrid* grid, const JmgConfig* cfg, const double* phi0,
+                    const double* rhs, const JmgCoeffs* coeffs, double* phi_out,
+                    int64_t* count_out, void* workspace, size_t workspace_bytes,
+                    jmg_stream_t stream);
+
+/* Coefficient hierarchy into the workspace (compute_discretization and the D / lambda
+ * hierarchies, solver_2d.py:326-421; solver_3d.py:338-429). */
+int jmg_build_hierarchy(JmgPlan* plan, const JmgCoeffs* coeffs, void* workspace,
+                        size_t workspace_bytes, jmg_stream_t stream);
+
+/* Operator entry points on dense padded arrays of one level; they use the hierarchy
+ * built by jmg_build_hierarchy in the same workspace.
+ *  jmg_op_sweep:    red_black_gauss_seidel (solver_2d.py:670-692; solver_3d.py:679-706),
+ *                   in place on phi.
+ *  jmg_op_restrict: defect + restriction (solver_2d.py:616-647; solver_3d.py:622-652);
+ *                   writes the level+1 array rhs_c.
+ *  jmg_op_prolong:  phi += prolongate(phi_c) (solver_2d.py:612, 649-668;
+ *                   solver_3d.py:618, 654-677), in place on phi.
+ *  jmg_op_residual: defect field d = rhs - L_h phi on the interior (defect before
+ *                   restriction, solver_2d.py:632-642), zero frame.
+ *  jmg_op_coeff:    copies one coefficient array of a level out of the workspace
+ *                   (which: 0 = A_cc, 1 = x-face, 2 = y-face, 3 = z-face), dense padded. */
+int jmg_op_sweep(JmgPlan* plan, int level, double* phi, const double* rhs, void* workspace,
+                 size_t workspace_bytes, jmg_stream_t stream);
+int jmg_op_restrict(JmgPlan* plan, int level, const double* phi, const double* rhs,
+                    double* rhs_c, void* workspace, size_t workspace_bytes, jmg_stream_t stream);
+int jmg_op_prolong(JmgPlan* plan, int level, double* phi, const double* phi_c, void* workspace,
+                   size_t workspace_bytes, jmg_stream_t stream);
+int jmg_op_residual(JmgPlan* plan, int level, const double* phi, const double* rhs, double* d,
+                    void* workspace, size_t workspace_bytes, jmg_stream_t stream);
+int jmg_op_coeff(JmgPlan* plan, int level, int which, double* out, void* workspace,
+                 size_t workspace_bytes, jmg_stream_t stream);
+
+/* Relative residual ||rhs - L_h phi||_2 / ||rhs||_2 over interior indices 2..m, FP64,
+ * written to the device double *out (the measure the benchmark stops on). */
+int jmg_rel_residual(JmgPlan* plan, const double* phi, const double* rhs, double* out,
+                     void* workspace, size_t workspace_bytes, jmg_stream_t stream);
+
+/* do_BCs(arr) with rim 1 and zero values (boundary_handler_2d.py:3-30,
+ * boundary_handler_3d.py:3-35), in place on a dense padded device array. */
+int jmg_do_bcs(int ndim, const int32_t* shape, double* arr, jmg_stream_t stream);
+
+/* Runs nsweeps red-black sweeps in place on the level arrays already in the workspace
+ * (phi and rhs of that level as left by jmg_solve / jmg_op_*): the smoother of
+ * red_black_gauss_seidel (solver_2d.py:670-692) without copies, for timing it alone. */
+int jmg_op_smooth_ws(JmgPlan* plan, int level, int nsweeps, void* workspace, size_t workspace_bytes,
+                     jmg_stream_t stream);
+
+/* Kernel launches of one jmg_solve: the fixed part (copies, hierarchy, loop set-up) and
+ * the part repeated per loop iteration (one cycle plus its stopping test). No reference
+ * counterpart: it reports this library's launch schedule. */
+int jmg_plan_launch_counts(const JmgPlan* plan, int64_t* per_solve_fixed, int64_t* per_cycle);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* jmg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JMG_H */

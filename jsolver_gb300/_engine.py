@@ -1,0 +1,244 @@
+"""Host side of a solve: argument rules of the reference, plan/workspace caching, C-ABI calls.
+
+``solve`` mirrors ``Solver_2D.solve`` / ``Solver_3D.solve`` (jsolver/solver_2d.py:423-479,
+jsolver/solver_3d.py:431-486): the same validation order and messages (grid checks when
+the solver is constructed, then dtype, then shapes), the same scalar/array forms of
+``lam`` and ``D``, the same return value ``(phi, count)``.
+
+Return types follow the inputs: NumPy/Python inputs give a NumPy ``phi`` and a Python
+``int`` count (the call waits for the GPU, like ``block_until_ready``); CUDA-tensor inputs
+give a CUDA tensor and, in dynamic mode, a 0-d int64 CUDA tensor count without any host
+synchronisation (fixed mode returns ``max_iters_outer`` as an int, as the reference does).
+"""
+import ctypes
+import threading
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._arrays import (is_cuda_tensor, is_float64, is_scalar, pick_device, scalar_value, shape_of,
+                      to_device)
+
+INT32_MAX = int(np.iinfo(np.int32).max)
+
+_PREC = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
+_STOP = {"distance": _lib.STOP_DISTANCE, "residual": _lib.STOP_RESIDUAL}
+
+
+def make_config(fixed=False, epsilon=1e-12, gamma=1, fcycle=False, skip_pre=False, nu1=1, nu2=1,
+                max_iters_outer=INT32_MAX, max_iters_inner=INT32_MAX, stop="distance", rtol=1e-10,
+                precision="fp64", inner_cycles=1):
+    c = _lib.default_config()
+    c.fixed = int(bool(fixed))
+    c.epsilon = float(epsilon)
+    c.gamma = int(gamma)
+    c.fcycle = int(bool(fcycle))
+    c.skip_pre = int(bool(skip_pre))
+    c.nu1 = int(nu1)
+    c.nu2 = int(nu2)
+    c.max_iters_outer = int(max_iters_outer)
+    c.max_iters_inner = int(max_iters_inner)
+    if stop not in _STOP:
+        raise ValueError(f"stop must be one of {sorted(_STOP)}, got {stop!r}")
+    if precision not in _PREC:
+        raise ValueError(f"precision must be one of {sorted(_PREC)}, got {precision!r}")
+    c.stop = _STOP[stop]
+    c.rtol = float(rtol)
+    c.precision = _PREC[precision]
+    c.inner_cycles = int(inner_cycles)
+    return c
+
+
+def make_grid(grids):
+    g = _lib.JmgGrid()
+    g.ndim = len(grids)
+    for a, gr in enumerate(grids):
+        g.m[a] = int(gr.mx)
+        g.idel[a] = float(gr.idel)
+        g.is_linear[a] = int(bool(gr.is_linear))
+    return g
+
+
+def _cfg_key(c):
+    return tuple(getattr(c, f) for f, _ in c._fields_)
+
+
+def _grid_key(g):
+    return (g.ndim, tuple(g.m), tuple(g.idel), tuple(g.is_linear))
+
+
+class _Cache:
+    """Plans (with their captured graphs) and workspaces, reused across calls."""
+
+    def __init__(self):
+        self.lock = threading.Lock()
+        self.plans = {}
+        self.ws = {}
+
+    def plan(self, grid, cfg):
+        key = (_grid_key(grid), _cfg_key(cfg))
+        with self.lock:
+            p = self.plans.get(key)
+            if p is None:
+                p = _lib.Plan(grid, cfg)
+                self.plans[key] = p
+            return p
+
+    def workspace(self, plan, device):
+        key = (id(plan), str(device))
+        with self.lock:
+            w = self.ws.get(key)
+            if w is None or w.numel() < plan.workspace_bytes:
+                w = torch.empty(max(plan.workspace_bytes, 1), dtype=torch.uint8, device=device)
+                self.ws[key] = w
+            return w
+
+
+CACHE = _Cache()
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def _stream_ptr(device):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def validate(ndim, phi, rhs, lam, D, D_xy, expected_shape):
+    """dtype and shape rules of solver_2d.py:444-453 / solver_3d.py:452-460."""
+    args = [phi, rhs, lam] + list(D) + ([] if D_xy is None else [D_xy])
+    if not all(is_float64(a) for a in args):
+        raise ValueError("Incorrect configuration: dtype must be 'jnp.float64' for all arguments.")
+    s = shape_of
+    sl = is_scalar(lam)
+    spatial = not all(is_scalar(d) for d in D)
+    off = ndim == 2 and spatial and D_xy is not None
+    same_D = all(s(d) == s(D[0]) for d in D)
+    bad = (not same_D or (sl and not s(phi) == s(rhs)) or (not sl and not s(phi) == s(rhs) == s(lam))
+           or (spatial and not all(s(phi) == s(x) for x in [rhs] + list(D)))
+           or (off and not s(phi) == s(D_xy)) or s(phi) != tuple(expected_shape))
+    if bad:
+        names = ["D_xx", "D_yy", "D_zz"][:ndim]
+        dstr = ", ".join(f"{n}={s(d)}" for n, d in zip(names, D))
+        tail = f", D_xy={'None' if D_xy is None else s(D_xy)}" if ndim == 2 else ""
+        raise ValueError(f"Shape mismatch: phi={s(phi)}, rhs={s(rhs)}, lam={s(lam)}, {dstr}{tail}.")
+    return sl, spatial, off
+
+
+def expected_shape(grids):
+    return tuple(int(g.mx) + 3 for g in reversed(grids))
+
+
+class Prepared:
+    """Device-side arguments of one call (keeps the tensors alive)."""
+
+    def __init__(self, ndim, device, lam, D, D_xy, sl, spatial):
+        self.coeffs = _lib.JmgCoeffs()
+        self.keep = []
+        if sl:
+            self.coeffs.lam = None
+            self.coeffs.lam_scalar = scalar_value(lam)
+        else:
+            t = to_device(lam, device)
+            self.keep.append(t)
+            self.coeffs.lam = t.data_ptr()
+        for a in range(ndim):
+            if spatial:
+                t = to_device(D[a], device)
+                self.keep.append(t)
+                self.coeffs.D[a] = t.data_ptr()
+            else:
+                self.coeffs.D[a] = None
+                self.coeffs.D_scalar[a] = scalar_value(D[a])
+        self.coeffs.D_xy = None
+
+
+def solve(grids, phi, rhs, lam, D, D_xy=None, **opts):
+    """Full solve through ``jmg_solve``. ``grids`` is (grid_x, grid_y[, grid_z])."""
+    ndim = len(grids)
+    cfg = make_config(**opts)
+    grid = make_grid(grids)
+    plan = CACHE.plan(grid, cfg)  # grid checks first (Solver_2D.__init__)
+    sl, spatial, off = validate(ndim, phi, rhs, lam, D, D_xy, expected_shape(grids))
+    if off:
+        raise NotImplementedError("spatially varying D with D_xy (9-point stencil) is not implemented on the GPU yet")
+    torch_in = any(is_cuda_tensor(a) for a in [phi, rhs, lam] + list(D))
+    device = pick_device(phi, rhs, lam, *D)
+    _lib.load()
+    with torch.cuda.device(device):
+        phi_d = to_device(phi, device)
+        rhs_d = to_device(rhs, device)
+        prep = Prepared(ndim, device, lam, D, D_xy, sl, spatial)
+        out = torch.empty_like(phi_d)
+        count = torch.empty((), dtype=torch.int64, device=device)
+        ws = CACHE.workspace(plan, device)
+        _lib.check(_lib.load().jmg_solve(plan.handle, _ptr(phi_d), _ptr(rhs_d), ctypes.byref(prep.coeffs),
+                                         _ptr(out), _ptr(count), _ptr(ws), ctypes.c_size_t(ws.numel()),
+                                         _stream_ptr(device)))
+        if torch_in:
+            return out, (int(cfg.max_iters_outer) if cfg.fixed else count)
+        return out.cpu().numpy(), (int(cfg.max_iters_outer) if cfg.fixed else int(count.item()))
+
+
+class OperatorSet:
+    """Level operators of one problem (reference Solver methods) on CUDA tensors."""
+
+    def __init__(self, grids, lam, D, D_xy=None, **opts):
+        self.ndim = len(grids)
+        self.grids = grids
+        self.cfg = make_config(**opts)
+        self.plan = _lib.Plan(make_grid(grids), self.cfg)
+        sl, spatial, off = validate(self.ndim, np.zeros(expected_shape(grids)), np.zeros(expected_shape(grids)),
+                                    lam, D, D_xy, expected_shape(grids))
+        if off:
+            raise NotImplementedError("D_xy (9-point stencil) is not implemented on the GPU yet")
+        self.device = pick_device(lam, *D)
+        self.prep = Prepared(self.ndim, self.device, lam, D, D_xy, sl, spatial)
+        self.ws = torch.empty(max(self.plan.workspace_bytes, 1), dtype=torch.uint8, device=self.device)
+        self.lib = _lib.load()
+        _lib.check(self.lib.jmg_build_hierarchy(self.plan.handle, ctypes.byref(self.prep.coeffs), _ptr(self.ws),
+                                                ctypes.c_size_t(self.ws.numel()), _stream_ptr(self.device)))
+        ms = [int(g.mx) for g in grids]
+        self.shapes = [tuple((m >> l) + 3 for m in reversed(ms)) for l in range(self.plan.levels)]
+
+    def _t(self, x):
+        return to_device(x, self.device).clone()
+
+    def _args(self):
+        return _ptr(self.ws), ctypes.c_size_t(self.ws.numel()), _stream_ptr(self.device)
+
+    def sweep(self, phi, rhs, level=0):
+        p = self._t(phi)
+        r = self._t(rhs)
+        _lib.check(self.lib.jmg_op_sweep(self.plan.handle, level, _ptr(p), _ptr(r), *self._args()))
+        return p
+
+    def restrict(self, phi, rhs, level):
+        p, r = self._t(phi), self._t(rhs)
+        out = torch.zeros(self.shapes[level + 1], dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.jmg_op_restrict(self.plan.handle, level, _ptr(p), _ptr(r), _ptr(out), *self._args()))
+        return out
+
+    def prolong_add(self, phi, phi_c, level):
+        p, c = self._t(phi), self._t(phi_c)
+        _lib.check(self.lib.jmg_op_prolong(self.plan.handle, level, _ptr(p), _ptr(c), *self._args()))
+        return p
+
+    def residual(self, phi, rhs, level=0):
+        p, r = self._t(phi), self._t(rhs)
+        out = torch.empty(self.shapes[level], dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.jmg_op_residual(self.plan.handle, level, _ptr(p), _ptr(r), _ptr(out), *self._args()))
+        return out
+
+    def coeff(self, level, which):
+        out = torch.empty(self.shapes[level], dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.jmg_op_coeff(self.plan.handle, level, which, _ptr(out), *self._args()))
+        return out
+
+    def rel_residual(self, phi, rhs):
+        p, r = self._t(phi), self._t(rhs)
+        out = torch.empty((), dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.jmg_rel_residual(self.plan.handle, _ptr(p), _ptr(r), _ptr(out), *self._args()))
+        return out

@@ -1,0 +1,234 @@
+// mg_common.cuh — level descriptors and per-point stencil arithmetic of the solver.
+//
+// Internal layout in the workspace: every level l keeps its padded arrays
+// ((m_y+3) x (m_x+3) in 2D, (m_z+3) x (m_y+3) x (m_x+3) in 3D, the reference's shapes,
+// solver_2d.py:302 / solver_3d.py:310) with a row pitch P rounded up to 16 elements, so
+// that rows start on 128-byte boundaries, and plane stride S = P * (m_y+3).
+//
+// Coefficients are stored as face arrays plus the diagonal, which is the reference's
+// AMat_* set (solver_2d.py:403-409; solver_3d.py:413-422) without duplication:
+//   wx[p] = coupling between p and p+1 (x),  A_lc(p) = wx[p-1], A_rc(p) = wx[p]
+//   wy[p] = coupling between p and p+P (y),  A_cl(p) = wy[p-P], A_cr(p) = wy[p]
+//   wz[p] = coupling between p and p+S (z),  A_ccl(p) = wz[p-S], A_ccr(p) = wz[p]
+//   acc[p] = A_cc(p), invd[p] = 1 / A_cc(p)
+// Interior unknowns are indices 2..m on every axis; the frame {0, 1, m+1, m+2} is zero
+// in phi and rhs at all times (do_BCs, boundary_handler_2d.py:21-30).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace jmg {
+
+template <typename T>
+struct Lvl {
+  T* phi;
+  T* rhs;
+  T* wx;
+  T* wy;
+  T* wz;
+  T* invd;
+  T* acc;
+  int mx, my, mz;  // resolution per axis (interior indices 2..m)
+  int P;           // row pitch in elements
+  long long S;     // plane stride in elements (3D)
+};
+
+constexpr int kMaxLevels = 16;
+
+template <typename T>
+struct LvlTable {
+  Lvl<T> l[kMaxLevels];
+};
+
+// Red (first) colour of a full sweep. In 2D the reference's first two sub-lattices
+// (0,0),(1,1) (solver_2d.py:684) are the points with i+j even; in 3D the first four,
+// (0,0,0),(0,1,1),(1,1,0),(1,0,1) (solver_3d.py:693), are the points with i+j+k odd.
+// Sub-lattices of one colour never neighbour each other, so updating a colour at
+// once is the same arithmetic as the reference's sequence of strided updates.
+template <int DIM>
+__host__ __device__ constexpr int first_color_parity() { return DIM == 2 ? 0 : 1; }
+
+// ---- 2D -------------------------------------------------------------------------------
+
+// Gauss-Seidel value of one interior point (solver_2d.py:687):
+//   (A_cr phi_N + A_cl phi_S + A_rc phi_E + A_lc phi_W - rhs) / A_cc
+template <typename T>
+__device__ __forceinline__ T gs_point2d(const T* __restrict__ ph, const T* __restrict__ rhs,
+                                        const T* __restrict__ wx, const T* __restrict__ wy,
+                                        const T* __restrict__ invd, long long p, int P) {
+  T s = wy[p] * ph[p + P];
+  s = fma(wy[p - P], ph[p - P], s);
+  s = fma(wx[p], ph[p + 1], s);
+  s = fma(wx[p - 1], ph[p - 1], s);
+  s = s - rhs[p];
+  return s * invd[p];
+}
+
+// Defect rhs - L_h phi at one interior point (solver_2d.py:637):
+//   A_cc phi - A_lc phi_W - A_rc phi_E - A_cl phi_S - A_cr phi_N + rhs
+template <typename T>
+__device__ __forceinline__ T defect_point2d(const T* ph, const T* rhs, const T* __restrict__ wx,
+                                            const T* __restrict__ wy, const T* __restrict__ acc,
+                                            long long p, int P) {
+  T d = acc[p] * ph[p];
+  d = fma(-wx[p - 1], ph[p - 1], d);
+  d = fma(-wx[p], ph[p + 1], d);
+  d = fma(-wy[p - P], ph[p - P], d);
+  d = fma(-wy[p], ph[p + P], d);
+  return d + rhs[p];
+}
+
+// Coarse right-hand side at coarse interior point (J, I) from the fine defects at the
+// red points (solver_2d.py:644): 1/16 of the four diagonal neighbours + 1/4 centre.
+template <typename T>
+__device__ __forceinline__ T restrict_point2d(const Lvl<T>& f, int J, int I) {
+  const int P = f.P;
+  const long long c = (long long)(2 * J - 1) * P + (2 * I - 1);
+  const T dne = defect_point2d(f.phi, f.rhs, f.wx, f.wy, f.acc, c + P + 1, P);
+  const T dnw = defect_point2d(f.phi, f.rhs, f.wx, f.wy, f.acc, c + P - 1, P);
+  const T dse = defect_point2d(f.phi, f.rhs, f.wx, f.wy, f.acc, c - P + 1, P);
+  const T dsw = defect_point2d(f.phi, f.rhs, f.wx, f.wy, f.acc, c - P - 1, P);
+  const T dc = defect_point2d(f.phi, f.rhs, f.wx, f.wy, f.acc, c, P);
+  const T s = ((dne + dnw) + dse) + dsw;
+  return T(0.0625) * s + T(0.25) * dc;
+}
+
+// Prolongated correction at fine interior point (i, j) (solver_2d.py:662-666).
+// Returns false for (even, even) points when they are skipped (nu2 > 0, no D_xy).
+template <typename T>
+__device__ __forceinline__ bool prolong_point2d(const Lvl<T>& c, int i, int j, bool diag, T* out) {
+  const T* pc = c.phi;
+  const int P = c.P;
+  const bool io = i & 1, jo = j & 1;
+  if (io && jo) {
+    *out = pc[(long long)((i + 1) >> 1) * P + ((j + 1) >> 1)];
+  } else if (io) {  // odd row, even column: linear in x
+    const long long r = (long long)((i + 1) >> 1) * P;
+    *out = T(0.5) * (pc[r + ((j + 2) >> 1)] + pc[r + (j >> 1)]);
+  } else if (jo) {  // even row, odd column: linear in y
+    const int cj = (j + 1) >> 1;
+    *out = T(0.5) * (pc[(long long)((i + 2) >> 1) * P + cj] + pc[(long long)(i >> 1) * P + cj]);
+  } else {
+    if (!diag) return false;
+    const long long rp = (long long)((i + 2) >> 1) * P, rm = (long long)(i >> 1) * P;
+    const int cp = (j + 2) >> 1, cm = j >> 1;
+    *out = T(0.25) * (((pc[rp + cp] + pc[rm + cp]) + pc[rp + cm]) + pc[rm + cm]);
+  }
+  return true;
+}
+
+// ---- 3D -------------------------------------------------------------------------------
+
+// (A_ccr U + A_ccl D + A_crc N + A_clc S + A_rcc E + A_lcc W - rhs) / A_ccc
+// (solver_3d.py:695-698)
+template <typename T>
+__device__ __forceinline__ T gs_point3d(const T* __restrict__ ph, const T* __restrict__ rhs,
+                                        const T* __restrict__ wx, const T* __restrict__ wy,
+                                        const T* __restrict__ wz, const T* __restrict__ invd,
+                                        long long p, int P, long long S) {
+  T s = wz[p] * ph[p + S];
+  s = fma(wz[p - S], ph[p - S], s);
+  s = fma(wy[p], ph[p + P], s);
+  s = fma(wy[p - P], ph[p - P], s);
+  s = fma(wx[p], ph[p + 1], s);
+  s = fma(wx[p - 1], ph[p - 1], s);
+  s = s - rhs[p];
+  return s * invd[p];
+}
+
+// A_ccc C - A_lcc W - A_rcc E - A_clc S - A_crc N - A_ccl D - A_ccr U + rhs
+// (solver_3d.py:642)
+template <typename T>
+__device__ __forceinline__ T defect_point3d(const T* ph, const T* rhs, const T* __restrict__ wx,
+                                            const T* __restrict__ wy, const T* __restrict__ wz,
+                                            const T* __restrict__ acc, long long p, int P,
+                                            long long S) {
+  T d = acc[p] * ph[p];
+  d = fma(-wx[p - 1], ph[p - 1], d);
+  d = fma(-wx[p], ph[p + 1], d);
+  d = fma(-wy[p - P], ph[p - P], d);
+  d = fma(-wy[p], ph[p + P], d);
+  d = fma(-wz[p - S], ph[p - S], d);
+  d = fma(-wz[p], ph[p + S], d);
+  return d + rhs[p];
+}
+
+// Coarse rhs at (K, J, I): 1/32 of the 12 edge-diagonal red neighbours + 1/8 centre,
+// summed in the reference's order (solver_3d.py:649).
+template <typename T>
+__device__ __forceinline__ T restrict_point3d(const Lvl<T>& f, int K, int J, int I) {
+  const int P = f.P;
+  const long long S = f.S;
+  const long long c = (long long)(2 * K - 1) * S + (long long)(2 * J - 1) * P + (2 * I - 1);
+#define JMG_D3(o) defect_point3d(f.phi, f.rhs, f.wx, f.wy, f.wz, f.acc, c + (o), P, S)
+  T s = JMG_D3(P + 1);
+  s = s + JMG_D3(P - 1);
+  s = s + JMG_D3(-P + 1);
+  s = s + JMG_D3(-P - 1);
+  s = s + JMG_D3(S + 1);
+  s = s + JMG_D3(S - 1);
+  s = s + JMG_D3(-S + 1);
+  s = s + JMG_D3(-S - 1);
+  s = s + JMG_D3(S + P);
+  s = s + JMG_D3(S - P);
+  s = s + JMG_D3(-S + P);
+  s = s + JMG_D3(-S - P);
+  const T dc = JMG_D3(0);
+#undef JMG_D3
+  return T(0.03125) * s + T(0.125) * dc;
+}
+
+// Prolongated correction at fine interior (k, j, i) (solver_3d.py:667-675). Points with
+// exactly two even indices are the bilinear ones, computed only when nu2 <= 0.
+template <typename T>
+__device__ __forceinline__ bool prolong_point3d(const Lvl<T>& c, int k, int j, int i, bool bilinear,
+                                                T* out) {
+  const T* pc = c.phi;
+  const int P = c.P;
+  const long long S = c.S;
+  const int ke = !(k & 1), je = !(j & 1), ie = !(i & 1);
+  const int ne = ke + je + ie;
+  // coarse indices: odd fine f -> (f+1)/2; even fine f -> (f+2)/2 ('+') and f/2 ('-')
+  const int kp = ke ? (k + 2) >> 1 : (k + 1) >> 1, km = ke ? (k >> 1) : kp;
+  const int jp = je ? (j + 2) >> 1 : (j + 1) >> 1, jm = je ? (j >> 1) : jp;
+  const int ip = ie ? (i + 2) >> 1 : (i + 1) >> 1, im = ie ? (i >> 1) : ip;
+#define JMG_C3(a, b, d) pc[(long long)(a) * S + (long long)(b) * P + (d)]
+  if (ne == 0) {
+    *out = JMG_C3(kp, jp, ip);
+  } else if (ne == 1) {
+    if (ie) *out = T(0.5) * (JMG_C3(kp, jp, ip) + JMG_C3(kp, jp, im));
+    else if (je) *out = T(0.5) * (JMG_C3(kp, jp, ip) + JMG_C3(kp, jm, ip));
+    else *out = T(0.5) * (JMG_C3(kp, jp, ip) + JMG_C3(km, jp, ip));
+  } else if (ne == 2) {
+    if (!bilinear) return false;
+    if (!ke)  // x and y even
+      *out = T(0.25) * (((JMG_C3(kp, jp, ip) + JMG_C3(kp, jm, ip)) + JMG_C3(kp, jp, im)) + JMG_C3(kp, jm, im));
+    else if (!je)  // x and z even
+      *out = T(0.25) * (((JMG_C3(kp, jp, ip) + JMG_C3(km, jp, ip)) + JMG_C3(kp, jp, im)) + JMG_C3(km, jp, im));
+    else  // y and z even
+      *out = T(0.25) * (((JMG_C3(kp, jp, ip) + JMG_C3(km, jp, ip)) + JMG_C3(kp, jm, ip)) + JMG_C3(km, jm, ip));
+  } else {
+    T s = JMG_C3(kp, jp, ip);
+    s = s + JMG_C3(km, jp, ip);
+    s = s + JMG_C3(kp, jm, ip);
+    s = s + JMG_C3(km, jm, ip);
+    s = s + JMG_C3(kp, jp, im);
+    s = s + JMG_C3(km, jp, im);
+    s = s + JMG_C3(kp, jm, im);
+    s = s + JMG_C3(km, jm, im);
+    *out = T(0.125) * s;
+  }
+#undef JMG_C3
+  return true;
+}
+
+// Order-preserving bit pattern of |x| for NaN-propagating max reductions: for
+// non-negative doubles the IEEE bit pattern is monotone, and a NaN (sign cleared)
+// compares above +inf, so the maximum is NaN whenever any difference is NaN. This
+// keeps the reference's rule that a NaN distance ends the dynamic loop
+// (jnp.max propagates NaN; NaN > epsilon is false).
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+}
+
+}  // namespace jmg

@@ -1,0 +1,712 @@
+// mg_driver.cu — plan, workspace layout, cycle schedule, CUDA graph and the C ABI.
+//
+// A solve (Solver_2D.solve, solver_2d.py:423-479; Solver_3D.solve, solver_3d.py:431-486)
+// runs as:
+//   1. copy phi0 / rhs from the caller's dense arrays into the pitched level-0 arrays
+//   2. coefficient hierarchy (mg_hierarchy.cu), one pass pair per level
+//   3. optional pre-smoothing (skip_pre, solver_2d.py:457-459)
+//   4. one launch of a CUDA graph: [loop init] -> WHILE(cond) { cycle; distance or
+//      residual; loop step }. The cycle is the reference's recursion (solver_2d.py:582-614)
+//      unrolled on the host into grid-wide kernel launches for the fine levels and one
+//      single-block kernel for every visit of the first coarse level, exactly as the JIT
+//      trace of the reference unrolls it into XLA ops.
+//   5. copy phi back to the caller's dense array; the cycle count goes to a device int64.
+// The graph is captured once per (plan, workspace address) and cached in the plan.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/jmg.h"
+#include "mg_kernels.h"
+
+using namespace jmg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_err(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define JMG_CUDA(call)                                                                          \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) return set_err(JMG_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t x, size_t a = kAlign) { return (x + a - 1) / a * a; }
+
+struct LevelInfo {
+  int m[3];
+  Box box;
+  size_t elems;
+  size_t phi, rhs, wx, wy, wz, invd, acc;   // FP64 arrays (byte offsets)
+  size_t d[3];                              // 3D averaged D (levels >= 1)
+  size_t phi32, rhs32, wx32, wy32, wz32, invd32, acc32;  // FP32 mirrors (mixed precision)
+};
+
+}  // namespace
+
+struct JmgPlan {
+  JmgGrid grid;
+  JmgConfig cfg;
+  int dim = 2;
+  int levels = 0;       // L of the reference
+  int used = 0;         // levels visited: 0..L-2
+  int coarse_start = 0; // first level run by the single-block kernel
+  bool mixed = false;
+  std::vector<LevelInfo> lv;
+  size_t off_phi_old = 0, off_state = 0, off_parts = 0, ws_bytes = 0;
+  int nparts = 0;
+  // graph cache
+  cudaGraphExec_t exec = nullptr;
+  void* exec_ws = nullptr;
+  int exec_mode = -1;
+  cudaStream_t cap = nullptr;
+};
+
+namespace {
+
+int validate_and_layout(JmgPlan* p) {
+  const JmgGrid& g = p->grid;
+  if (g.ndim != 2 && g.ndim != 3) return set_err(JMG_ERR_VALUE, "ndim must be 2 or 3, got %d", g.ndim);
+  const char* names[3] = {"x", "y", "z"};
+  const int d = g.ndim;
+  // power-of-two checks in x, y, z order (solver_2d.py:292-295; solver_3d.py:295-300)
+  for (int a = 0; a < d; ++a) {
+    const long long m = g.m[a];
+    if (m <= 0 || (m & (m - 1)) != 0)
+      return set_err(JMG_ERR_VALUE, "Resolution of %s-grid is not a power of 2. Value: %lld", names[a], m);
+  }
+  int lv[3];
+  int L = 1 << 30;
+  for (int a = 0; a < d; ++a) {
+    lv[a] = (int)std::ceil(std::log2((double)g.m[a])) + 1;
+    L = lv[a] < L ? lv[a] : L;
+  }
+  // efficiency checks (solver_2d.py:304-307; solver_3d.py:312-317)
+  for (int a = 0; a < d; ++a) {
+    const long long coarsest = 1LL << (lv[a] - L);
+    if (coarsest > 5)
+      return set_err(JMG_ERR_VALUE,
+                     "Resolution of %s-grid not efficient for multigrid configuration. Resolution of coarsest level: %lld",
+                     names[a], coarsest);
+  }
+  // linear grids only (solver_2d.py:320-321; solver_3d.py:331-332)
+  for (int a = 0; a < d; ++a)
+    if (!g.is_linear[a]) return set_err(JMG_ERR_VALUE, "Only linear grids are supported!");
+  if (L < 2)
+    return set_err(JMG_ERR_VALUE,
+                   "Resolution too small for multigrid: the smallest axis needs at least 2 cells (got levels=%d)", L);
+  if (L > kMaxLevels + 1) return set_err(JMG_ERR_VALUE, "too many levels (%d)", L);
+  p->dim = d;
+  p->levels = L;
+  p->used = L - 1;
+  p->mixed = p->cfg.precision == JMG_PREC_MIXED;
+  p->lv.resize(p->used);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off = align_up(off + bytes);
+    return o;
+  };
+  for (int l = 0; l < p->used; ++l) {
+    LevelInfo& li = p->lv[l];
+    for (int a = 0; a < 3; ++a) li.m[a] = a < d ? (int)(g.m[a] >> l) : 0;
+    li.box.nx = li.m[0] + 3;
+    li.box.ny = li.m[1] + 3;
+    li.box.nz = d == 3 ? li.m[2] + 3 : 1;
+    li.box.P = (li.box.nx + 15) / 16 * 16;
+    li.box.S = (long long)li.box.P * li.box.ny;
+    li.elems = (size_t)li.box.S * li.box.nz;
+    const size_t b8 = li.elems * 8, b4 = li.elems * 4;
+    li.phi = take(b8);
+    li.rhs = take(b8);
+    li.wx = take(b8);
+    li.wy = take(b8);
+    li.wz = d == 3 ? take(b8) : 0;
+    li.invd = take(b8);
+    li.acc = take(b8);
+    for (int c = 0; c < 3; ++c) li.d[c] = (d == 3 && l >= 1) ? take(b8) : 0;
+    if (p->mixed) {
+      li.phi32 = take(b4);
+      li.rhs32 = take(b4);
+      li.wx32 = take(b4);
+      li.wy32 = take(b4);
+      li.wz32 = d == 3 ? take(b4) : 0;
+      li.invd32 = take(b4);
+      li.acc32 = take(b4);
+    }
+  }
+  p->off_phi_old = take(p->lv[0].elems * 8);
+  p->off_state = take(sizeof(LoopState));
+  p->nparts = residual_num_parts(d, p->lv[0].box);
+  p->off_parts = take((size_t)p->nparts * 8 + 64);
+  p->ws_bytes = off;
+  // coarse levels: at most 8192 padded points, and never below the last visited level
+  int cs = p->used - 1;
+  for (int l = 0; l < p->used; ++l) {
+    const long long pts = (long long)p->lv[l].box.nx * p->lv[l].box.ny * p->lv[l].box.nz;
+    if (pts <= 8192) {
+      cs = l;
+      break;
+    }
+  }
+  p->coarse_start = cs;
+  return JMG_OK;
+}
+
+template <typename T>
+T* ptr(void* ws, size_t off) {
+  return reinterpret_cast<T*>(static_cast<char*>(ws) + off);
+}
+
+Lvl<double> lvl64(const JmgPlan* p, void* ws, int l) {
+  const LevelInfo& li = p->lv[l];
+  Lvl<double> a;
+  a.phi = ptr<double>(ws, li.phi);
+  a.rhs = ptr<double>(ws, li.rhs);
+  a.wx = ptr<double>(ws, li.wx);
+  a.wy = ptr<double>(ws, li.wy);
+  a.wz = p->dim == 3 ? ptr<double>(ws, li.wz) : nullptr;
+  a.invd = ptr<double>(ws, li.invd);
+  a.acc = ptr<double>(ws, li.acc);
+  a.mx = li.m[0];
+  a.my = li.m[1];
+  a.mz = li.m[2];
+  a.P = li.box.P;
+  a.S = li.box.S;
+  return a;
+}
+
+Lvl<float> lvl32(const JmgPlan* p, void* ws, int l) {
+  const LevelInfo& li = p->lv[l];
+  Lvl<float> a;
+  a.phi = ptr<float>(ws, li.phi32);
+  a.rhs = ptr<float>(ws, li.rhs32);
+  a.wx = ptr<float>(ws, li.wx32);
+  a.wy = ptr<float>(ws, li.wy32);
+  a.wz = p->dim == 3 ? ptr<float>(ws, li.wz32) : nullptr;
+  a.invd = ptr<float>(ws, li.invd32);
+  a.acc = ptr<float>(ws, li.acc32);
+  a.mx = li.m[0];
+  a.my = li.m[1];
+  a.mz = li.m[2];
+  a.P = li.box.P;
+  a.S = li.box.S;
+  return a;
+}
+
+template <typename T>
+LvlTable<T> make_table(const JmgPlan* p, void* ws);
+template <>
+LvlTable<double> make_table<double>(const JmgPlan* p, void* ws) {
+  LvlTable<double> t;
+  memset(&t, 0, sizeof(t));
+  for (int l = 0; l < p->used; ++l) t.l[l] = lvl64(p, ws, l);
+  return t;
+}
+template <>
+LvlTable<float> make_table<float>(const JmgPlan* p, void* ws) {
+  LvlTable<float> t;
+  memset(&t, 0, sizeof(t));
+  for (int l = 0; l < p->used; ++l) t.l[l] = lvl32(p, ws, l);
+  return t;
+}
+
+CycleParams cycle_params(const JmgPlan* p, bool off_diag) {
+  CycleParams cp;
+  cp.last_level = p->levels - 2;
+  cp.nu1 = p->cfg.nu1 > 0 ? p->cfg.nu1 : 0;
+  cp.nu2 = p->cfg.nu2 > 0 ? p->cfg.nu2 : 0;
+  cp.gamma = p->cfg.gamma > 0 ? p->cfg.gamma : 0;
+  // 2D: the (even,even) points need prolongation if nu2 <= 0 or with D_xy
+  // (solver_2d.py:665); 3D: the bilinear points if nu2 <= 0 (solver_3d.py:671)
+  cp.diag = (p->cfg.nu2 <= 0 || off_diag) ? 1 : 0;
+  return cp;
+}
+
+// multigrid_cycle, solver_2d.py:582-614, emitted as launches on stream s. With a
+// non-null `count`, nothing is launched and the number of kernel launches is added.
+template <typename T>
+void emit_cycle(const JmgPlan* p, const LvlTable<T>& tab, const CycleParams& cp, int lev, bool fcycle,
+                bool skip_pre, cudaStream_t s, long long* count = nullptr) {
+  const int dim = p->dim;
+  auto sweep = [&]() {
+    if (count) *count += 2;
+    else launch_sweep<T>(dim, tab.l[lev], s);
+  };
+  if (lev >= p->coarse_start) {
+    if (count) *count += 1;
+    else launch_coarse_cycle<T>(dim, tab, cp, lev, fcycle ? 1 : 0, skip_pre ? 1 : 0, s);
+    return;
+  }
+  if (lev == cp.last_level) {
+    for (int k = 0; k < cp.nu1 + cp.nu2; ++k) sweep();
+    return;
+  }
+  if (!skip_pre)
+    for (int k = 0; k < cp.nu1; ++k) sweep();
+  if (count) *count += 1;
+  else launch_restrict<T>(dim, tab.l[lev], tab.l[lev + 1], s);
+  if (fcycle)
+    for (int g = 0; g < cp.gamma; ++g) emit_cycle<T>(p, tab, cp, lev + 1, true, false, s, count);
+  for (int g = 0; g < cp.gamma; ++g) emit_cycle<T>(p, tab, cp, lev + 1, false, false, s, count);
+  if (count) *count += 1;
+  else launch_prolong<T>(dim, tab.l[lev], tab.l[lev + 1], cp.diag, s);
+  for (int k = 0; k < cp.nu2; ++k) sweep();
+}
+
+int loop_mode(const JmgPlan* p) {
+  if (p->cfg.fixed) return 2;
+  return p->cfg.stop == JMG_STOP_RESIDUAL ? 1 : 0;
+}
+
+// body of one loop iteration (captured into the WHILE node's body graph)
+void emit_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaStream_t s) {
+  const int mode = loop_mode(p);
+  LoopState* st = ptr<LoopState>(ws, p->off_state);
+  double* parts = ptr<double>(ws, p->off_parts);
+  Lvl<double> l0 = lvl64(p, ws, 0);
+  CycleParams cp = cycle_params(p, false);
+  if (!p->mixed) {
+    LvlTable<double> tab = make_table<double>(p, ws);
+    emit_cycle<double>(p, tab, cp, 0, p->cfg.fcycle != 0, p->cfg.skip_pre != 0, s);
+  } else {
+    // FP64 iterative refinement around FP32 cycles: r = rhs - L_h phi (FP64), solve
+    // L_h e = r with FP32 cycles from e = 0, phi += e (FP64)
+    LvlTable<float> t32 = make_table<float>(p, ws);
+    launch_residual_to_f32(p->dim, l0, t32.l[0].rhs, s);
+    launch_zero_f32(p->lv[0].box, t32.l[0].phi, s);
+    const int inner = p->cfg.inner_cycles > 0 ? p->cfg.inner_cycles : 1;
+    for (int k = 0; k < inner; ++k) emit_cycle<float>(p, t32, cp, 0, p->cfg.fcycle != 0, false, s);
+    launch_add_correction(p->dim, l0, t32.l[0].phi, s);
+  }
+  if (mode == 0) launch_distance_snapshot(p->lv[0].box, ptr<double>(ws, p->off_phi_old), l0.phi, st, s);
+  if (mode == 1) launch_residual_partials<double>(p->dim, l0, l0.phi, parts, p->nparts, s);
+  launch_loop_step(st, parts, p->nparts, mode, p->cfg.epsilon, p->cfg.rtol, p->cfg.max_iters_outer, handle, s);
+}
+
+long long body_launches(const JmgPlan* p) {
+  long long n = 0;
+  CycleParams cp = cycle_params(p, false);
+  if (!p->mixed) {
+    LvlTable<double> t;
+    memset(&t, 0, sizeof(t));
+    emit_cycle<double>(p, t, cp, 0, p->cfg.fcycle != 0, p->cfg.skip_pre != 0, nullptr, &n);
+  } else {
+    LvlTable<float> t;
+    memset(&t, 0, sizeof(t));
+    const int inner = p->cfg.inner_cycles > 0 ? p->cfg.inner_cycles : 1;
+    for (int k = 0; k < inner; ++k) emit_cycle<float>(p, t, cp, 0, p->cfg.fcycle != 0, false, nullptr, &n);
+    n += 3;  // residual_to_f32, zero, add_correction
+  }
+  const int mode = loop_mode(p);
+  if (mode == 0 || mode == 1) n += 1;  // distance or residual partials
+  n += 1;                              // loop step
+  return n;
+}
+
+int build_graph(JmgPlan* p, void* ws) {
+  if (p->exec && p->exec_ws == ws) return JMG_OK;
+  if (p->exec) {
+    cudaGraphExecDestroy(p->exec);
+    p->exec = nullptr;
+  }
+  if (!p->cap) JMG_CUDA(cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking));
+  const int mode = loop_mode(p);
+  LoopState* st = ptr<LoopState>(ws, p->off_state);
+  double* parts = ptr<double>(ws, p->off_parts);
+  Lvl<double> l0 = lvl64(p, ws, 0);
+
+  cudaGraph_t graph;
+  JMG_CUDA(cudaGraphCreate(&graph, 0));
+  cudaGraphConditionalHandle handle;
+  JMG_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 0, 0));
+  // prologue: initial residual (residual stop) and loop init, then the WHILE node
+  JMG_CUDA(cudaStreamBeginCaptureToGraph(p->cap, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  if (mode == 1) launch_residual_partials<double>(p->dim, l0, l0.phi, parts, p->nparts, p->cap);
+  launch_loop_init(st, parts, p->nparts, mode, p->cfg.rtol, p->cfg.max_iters_outer, handle, p->cap);
+  cudaStreamCaptureStatus cst;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  JMG_CUDA(cudaStreamGetCaptureInfo(p->cap, &cst, nullptr, nullptr, &deps, nullptr, &ndeps));
+  cudaGraphNodeParams cparams = {cudaGraphNodeTypeConditional};
+  cparams.conditional.handle = handle;
+  cparams.conditional.type = cudaGraphCondTypeWhile;
+  cparams.conditional.size = 1;
+  cudaGraphNode_t cnode;
+  JMG_CUDA(cudaGraphAddNode(&cnode, graph, deps, nullptr, ndeps, &cparams));
+  JMG_CUDA(cudaStreamUpdateCaptureDependencies(p->cap, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+  JMG_CUDA(cudaStreamEndCapture(p->cap, &graph));
+  cudaGraph_t body = cparams.conditional.phGraph_out[0];
+  JMG_CUDA(cudaStreamBeginCaptureToGraph(p->cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  emit_body(p, ws, (unsigned long long)handle, p->cap);
+  JMG_CUDA(cudaGetLastError());
+  cudaGraph_t body_out = body;
+  JMG_CUDA(cudaStreamEndCapture(p->cap, &body_out));
+  cudaGraphExec_t exec;
+  JMG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  cudaGraphDestroy(graph);
+  p->exec = exec;
+  p->exec_ws = ws;
+  p->exec_mode = mode;
+  return JMG_OK;
+}
+
+HierInputs hier_inputs(const JmgPlan* p, const JmgCoeffs* c) {
+  HierInputs in;
+  in.lam = c->lam;
+  in.lam_scalar = c->lam_scalar;
+  in.scalar_lam = c->lam == nullptr;
+  int nscalar = 0;
+  for (int a = 0; a < 3; ++a) {
+    in.D[a] = a < p->dim ? c->D[a] : nullptr;
+    in.D_scalar[a] = a < p->dim ? c->D_scalar[a] : 0.0;
+    if (a < p->dim && c->D[a] == nullptr) ++nscalar;
+  }
+  in.scalar_D = nscalar == p->dim;
+  return in;
+}
+
+int check_coeffs(const JmgPlan* p, const JmgCoeffs* c) {
+  if (!c) return set_err(JMG_ERR_VALUE, "coeffs must not be NULL");
+  int nscalar = 0;
+  for (int a = 0; a < p->dim; ++a)
+    if (c->D[a] == nullptr) ++nscalar;
+  if (nscalar != 0 && nscalar != p->dim)
+    return set_err(JMG_ERR_VALUE, "Shape mismatch: the D components must be all scalars or all arrays.");
+  if (c->D_xy && p->dim == 3) return set_err(JMG_ERR_VALUE, "D_xy is a 2D argument");
+  if (c->D_xy && nscalar == 0)
+    return set_err(JMG_ERR_VALUE, "D_xy (9-point stencil) is not supported by this build");
+  return JMG_OK;
+}
+
+int check_ws(const JmgPlan* p, void* ws, size_t bytes) {
+  if (!p) return set_err(JMG_ERR_VALUE, "plan must not be NULL");
+  if (!ws || bytes < p->ws_bytes)
+    return set_err(JMG_ERR_WORKSPACE, "workspace too small: %zu bytes given, %zu needed", bytes, p->ws_bytes);
+  if (reinterpret_cast<uintptr_t>(ws) % kAlign != 0)
+    return set_err(JMG_ERR_WORKSPACE, "workspace must be %zu-byte aligned", kAlign);
+  return JMG_OK;
+}
+
+int build_hierarchy(JmgPlan* p, const JmgCoeffs* c, void* ws, cudaStream_t s) {
+  const HierInputs in = hier_inputs(p, c);
+  const Box b0 = p->lv[0].box;
+  for (int l = 0; l < p->used; ++l) {
+    const LevelInfo& li = p->lv[l];
+    double sq[3];
+    for (int a = 0; a < 3; ++a) {
+      const double id = a < p->dim ? p->grid.idel[a] * std::pow(0.5, l) : 0.0;  // solver_2d.py:323
+      sq[a] = id * id;                                                         // solver_2d.py:395
+    }
+    double* dcur[3] = {nullptr, nullptr, nullptr};
+    const double* dprev[3] = {nullptr, nullptr, nullptr};
+    Box bprev = b0;
+    if (p->dim == 3 && l >= 1) {
+      for (int a = 0; a < 3; ++a) dcur[a] = ptr<double>(ws, li.d[a]);
+      if (l >= 2) {
+        for (int a = 0; a < 3; ++a) dprev[a] = ptr<double>(ws, p->lv[l - 1].d[a]);
+        bprev = p->lv[l - 1].box;
+      }
+    }
+    launch_hierarchy_level(p->dim, l, lvl64(p, ws, l), li.box, b0, in, sq, dcur, dprev, bprev, s);
+  }
+  if (p->mixed) {
+    for (int l = 0; l < p->used; ++l) {
+      const LevelInfo& li = p->lv[l];
+      Lvl<double> a = lvl64(p, ws, l);
+      Lvl<float> f = lvl32(p, ws, l);
+      launch_convert_f32(li.box, a.wx, f.wx, s);
+      launch_convert_f32(li.box, a.wy, f.wy, s);
+      if (p->dim == 3) launch_convert_f32(li.box, a.wz, f.wz, s);
+      launch_convert_f32(li.box, a.invd, f.invd, s);
+      launch_convert_f32(li.box, a.acc, f.acc, s);
+    }
+  }
+  JMG_CUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
+__global__ void k_write_i64(long long* out, long long v) { *out = v; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------------------
+
+extern "C" {
+
+void jmg_config_default(JmgConfig* c) {
+  memset(c, 0, sizeof(*c));
+  c->fixed = 0;
+  c->gamma = 1;
+  c->fcycle = 0;
+  c->skip_pre = 0;
+  c->nu1 = 1;
+  c->nu2 = 1;
+  c->max_iters_outer = 2147483647LL;
+  c->max_iters_inner = 2147483647LL;
+  c->epsilon = 1e-12;
+  c->stop = JMG_STOP_DISTANCE;
+  c->rtol = 1e-10;
+  c->precision = JMG_PREC_FP64;
+  c->inner_cycles = 1;
+}
+
+int jmg_plan_create(JmgPlan** out, const JmgGrid* grid, const JmgConfig* cfg) {
+  if (!out || !grid || !cfg) return set_err(JMG_ERR_VALUE, "NULL argument");
+  *out = nullptr;
+  JmgPlan* p = new JmgPlan();
+  p->grid = *grid;
+  p->cfg = *cfg;
+  const int rc = validate_and_layout(p);
+  if (rc != JMG_OK) {
+    delete p;
+    return rc;
+  }
+  *out = p;
+  g_last_error.clear();
+  return JMG_OK;
+}
+
+int jmg_plan_destroy(JmgPlan* p) {
+  if (!p) return JMG_OK;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->cap) cudaStreamDestroy(p->cap);
+  delete p;
+  return JMG_OK;
+}
+
+size_t jmg_plan_workspace_bytes(const JmgPlan* p) { return p ? p->ws_bytes : 0; }
+int jmg_plan_levels(const JmgPlan* p) { return p ? p->levels : 0; }
+
+int jmg_build_hierarchy(JmgPlan* p, const JmgCoeffs* c, void* ws, size_t bytes, jmg_stream_t stream) {
+  int rc = check_ws(p, ws, bytes);
+  if (rc) return rc;
+  if ((rc = check_coeffs(p, c))) return rc;
+  return build_hierarchy(p, c, ws, (cudaStream_t)stream);
+}
+
+int jmg_solve(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs* c, double* phi_out,
+              int64_t* count_out, void* ws, size_t bytes, jmg_stream_t stream) {
+  int rc = check_ws(p, ws, bytes);
+  if (rc) return rc;
+  if ((rc = check_coeffs(p, c))) return rc;
+  if (!phi0 || !rhs || !phi_out) return set_err(JMG_ERR_VALUE, "phi0, rhs and phi_out must not be NULL");
+  cudaStream_t s = (cudaStream_t)stream;
+  const Box b0 = p->lv[0].box;
+  Lvl<double> l0 = lvl64(p, ws, 0);
+  LoopState* st = ptr<LoopState>(ws, p->off_state);
+  double* parts = ptr<double>(ws, p->off_parts);
+  double* phi_old = ptr<double>(ws, p->off_phi_old);
+  const int mode = loop_mode(p);
+  // 1. inputs; phi_old keeps phi0 with its frame (the first distance sees it, solver_2d.py:471)
+  launch_copy_in(b0, phi0, l0.phi, 1, s);
+  launch_copy_in(b0, phi0, phi_old, 0, s);
+  launch_copy_in(b0, rhs, l0.rhs, 1, s);
+  // 2. coefficients
+  if ((rc = build_hierarchy(p, c, ws, s))) return rc;
+  if (mode == 1) {
+    launch_residual_partials<double>(p->dim, l0, nullptr, parts, p->nparts, s);
+    launch_rhs_norm(st, parts, p->nparts, s);
+  }
+  // 3. skip_pre: pre-smoothing once, before the loop (solver_2d.py:457-459)
+  const int nu1 = p->cfg.nu1 > 0 ? p->cfg.nu1 : 0;
+  const bool presmoothed = p->cfg.skip_pre && nu1 > 0;
+  if (presmoothed) {
+    for (int k = 0; k < nu1; ++k) launch_sweep<double>(p->dim, l0, s);
+    launch_distance_snapshot(b0, phi_old, l0.phi, st, s);  // phi_old <- smoothed phi
+  }
+  // 4. the loop
+  const bool runs = p->cfg.max_iters_outer > 0;
+  if (runs) {
+    if ((rc = build_graph(p, ws))) return rc;
+    JMG_CUDA(cudaGraphLaunch(p->exec, s));
+  }
+  // 5. outputs. With no cycle and no smoothing the reference returns phi0 untouched.
+  if (runs || presmoothed)
+    launch_copy_out(b0, l0.phi, phi_out, s);
+  else if (phi_out != phi0)
+    JMG_CUDA(cudaMemcpyAsync(phi_out, phi0, (size_t)b0.nx * b0.ny * b0.nz * 8, cudaMemcpyDeviceToDevice, s));
+  if (count_out) {
+    if (p->cfg.fixed || !runs)
+      k_write_i64<<<1, 1, 0, s>>>((long long*)count_out, p->cfg.fixed ? p->cfg.max_iters_outer : 0);
+    else
+      launch_count_out(st, (long long*)count_out, s);
+  }
+  JMG_CUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
+static int solve_oneshot(int dim, const JmgGrid* grid, const JmgConfig* cfg, const double* phi0, const double* rhs,
+                         const JmgCoeffs* c, double* phi_out, int64_t* count_out, void* ws, size_t bytes,
+                         jmg_stream_t stream) {
+  if (!grid || grid->ndim != dim) return set_err(JMG_ERR_VALUE, "grid->ndim must be %d", dim);
+  JmgPlan* p = nullptr;
+  int rc = jmg_plan_create(&p, grid, cfg);
+  if (rc) return rc;
+  rc = jmg_solve(p, phi0, rhs, c, phi_out, count_out, ws, bytes, stream);
+  if (rc == JMG_OK && p->exec) {
+    // the graph exec is destroyed with the plan: wait for the launch to finish first
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) rc = set_err(JMG_ERR_CUDA, "cudaStreamSynchronize failed: %s", cudaGetErrorString(e));
+  }
+  jmg_plan_destroy(p);
+  return rc;
+}
+
+int jmg_solve2d_f64(const JmgGrid* grid, const JmgConfig* cfg, const double* phi0, const double* rhs,
+                    const JmgCoeffs* c, double* phi_out, int64_t* count_out, void* ws, size_t bytes,
+                    jmg_stream_t stream) {
+  return solve_oneshot(2, grid, cfg, phi0, rhs, c, phi_out, count_out, ws, bytes, stream);
+}
+
+int jmg_solve3d_f64(const JmgGrid* grid, const JmgConfig* cfg, const double* phi0, const double* rhs,
+                    const JmgCoeffs* c, double* phi_out, int64_t* count_out, void* ws, size_t bytes,
+                    jmg_stream_t stream) {
+  return solve_oneshot(3, grid, cfg, phi0, rhs, c, phi_out, count_out, ws, bytes, stream);
+}
+
+static int level_check(const JmgPlan* p, int level, bool needs_coarse) {
+  if (level < 0 || level >= p->used || (needs_coarse && level + 1 >= p->used))
+    return set_err(JMG_ERR_VALUE, "level %d out of range", level);
+  return JMG_OK;
+}
+
+int jmg_op_sweep(JmgPlan* p, int level, double* phi, const double* rhs, void* ws, size_t bytes,
+                 jmg_stream_t stream) {
+  int rc = check_ws(p, ws, bytes);
+  if (rc || (rc = level_check(p, level, false))) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  Lvl<double> a = lvl64(p, ws, level);
+  const Box b = p->lv[level].box;
+  launch_copy_in(b, phi, a.phi, 1, s);  // the sweep starts with do_BCs (solver_2d.py:682)
+  launch_copy_in(b, rhs, a.rhs, 0, s);
+  launch_sweep<double>(p->dim, a, s);
+  launch_copy_out(b, a.phi, phi, s);
+  JMG_CUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
+int jmg_op_restrict(JmgPlan* p, int level, const double* phi, const double* rhs, double* rhs_c, void* ws,
+                    size_t bytes, jmg_stream_t stream) {
+  int rc = check_ws(p, ws, bytes);
+  if (rc || (rc = level_check(p, level, true))) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  Lvl<double> f = lvl64(p, ws, level), c = lvl64(p, ws, level + 1);
+  const Box b = p->lv[level].box;
+  launch_copy_in(b, phi, f.phi, 1, s);
+  launch_copy_in(b, rhs, f.rhs, 0, s);
+  launch_restrict<double>(p->dim, f, c, s);
+  launch_copy_out(p->lv[level + 1].box, c.rhs, rhs_c, s);
+  JMG_CUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
+int jmg_op_prolong(JmgPlan* p, int level, double* phi, const double* phi_c, void* ws, size_t bytes,
+                   jmg_stream_t stream) {
+  int rc = check_ws(p, ws, bytes);
+  if (rc || (rc = level_check(p, level, true))) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  Lvl<double> f = lvl64(p, ws, level), c = lvl64(p, ws, level + 1);
+  launch_copy_in(p->lv[level].box, phi, f.phi, 0, s);
+  launch_copy_in(p->lv[level + 1].box, phi_c, c.phi, 0, s);
+  launch_prolong<double>(p->dim, f, c, cycle_params(p, false).diag, s);
+  launch_copy_out(p->lv[level].box, f.phi, phi, s);
+  JMG_CUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
+int jmg_op_residual(JmgPlan* p, int level, const double* phi, const double* rhs, double* d, void* ws,
+                    size_t bytes, jmg_stream_t stream) {
+  int rc = check_ws(p, ws, bytes);
+  if (rc || (rc = level_check(p, level, false))) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  Lvl<double> a = lvl64(p, ws, level);
+  const Box b = p->lv[level].box;
+  launch_copy_in(b, phi, a.phi, 1, s);
+  launch_copy_in(b, rhs, a.rhs, 0, s);
+  launch_dense_residual(p->dim, a, b, d, s);
+  JMG_CUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
+int jmg_op_coeff(JmgPlan* p, int level, int which, double* out, void* ws, size_t bytes, jmg_stream_t stream) {
+  int rc = check_ws(p, ws, bytes);
+  if (rc || (rc = level_check(p, level, false))) return rc;
+  Lvl<double> a = lvl64(p, ws, level);
+  const double* src = which == 0 ? a.acc : which == 1 ? a.wx : which == 2 ? a.wy : which == 3 ? a.wz : nullptr;
+  if (!src) return set_err(JMG_ERR_VALUE, "no coefficient array %d in %dD", which, p->dim);
+  launch_copy_coeff(p->lv[level].box, src, out, (cudaStream_t)stream);
+  JMG_CUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
+int jmg_rel_residual(JmgPlan* p, const double* phi, const double* rhs, double* out, void* ws, size_t bytes,
+                     jmg_stream_t stream) {
+  int rc = check_ws(p, ws, bytes);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  Lvl<double> a = lvl64(p, ws, 0);
+  const Box b = p->lv[0].box;
+  LoopState* st = ptr<LoopState>(ws, p->off_state);
+  double* parts = ptr<double>(ws, p->off_parts);
+  launch_copy_in(b, phi, a.phi, 1, s);
+  launch_copy_in(b, rhs, a.rhs, 1, s);
+  launch_residual_partials<double>(p->dim, a, nullptr, parts, p->nparts, s);
+  launch_rhs_norm(st, parts, p->nparts, s);
+  launch_residual_partials<double>(p->dim, a, a.phi, parts, p->nparts, s);
+  launch_rel_residual_out(st, parts, p->nparts, out, s);
+  JMG_CUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
+int jmg_do_bcs(int ndim, const int32_t* shape, double* arr, jmg_stream_t stream) {
+  if (ndim != 2 && ndim != 3) return set_err(JMG_ERR_VALUE, "ndim must be 2 or 3");
+  launch_do_bcs_dense(ndim, shape, arr, (cudaStream_t)stream);
+  JMG_CUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
+int jmg_plan_launch_counts(const JmgPlan* p, int64_t* per_solve_fixed, int64_t* per_cycle) {
+  if (!p) return set_err(JMG_ERR_VALUE, "plan must not be NULL");
+  // copy-ins (3), hierarchy (2 per level + FP32 conversions), rhs norm (2), loop init
+  // (1-2), copy-out and count (2)
+  long long fixed = 3 + 2LL * p->used + 2 + 2;
+  if (p->mixed) fixed += (long long)p->used * (p->dim == 3 ? 5 : 4);
+  if (loop_mode(p) == 1) fixed += 2 + 1;
+  fixed += 1;
+  if (p->cfg.skip_pre) fixed += 2LL * (p->cfg.nu1 > 0 ? p->cfg.nu1 : 0) + 1;
+  if (per_solve_fixed) *per_solve_fixed = fixed;
+  if (per_cycle) *per_cycle = body_launches(p);
+  return JMG_OK;
+}
+
+int jmg_op_smooth_ws(JmgPlan* p, int level, int nsweeps, void* ws, size_t bytes, jmg_stream_t stream) {
+  int rc = check_ws(p, ws, bytes);
+  if (rc || (rc = level_check(p, level, false))) return rc;
+  Lvl<double> a = lvl64(p, ws, level);
+  for (int k = 0; k < nsweeps; ++k) launch_sweep<double>(p->dim, a, (cudaStream_t)stream);
+  JMG_CUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
+const char* jmg_last_error(void) { return g_last_error.c_str(); }
+
+}  // extern "C"

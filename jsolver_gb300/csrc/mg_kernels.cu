@@ -1,0 +1,251 @@
+// mg_kernels.cu — sm_103a kernels of the multigrid cycle (2D and 3D, FP64 and FP32).
+//
+// Grid-wide kernels, one launch per operator, run the fine levels:
+//   k_sweep_color   one colour of the red-black Gauss-Seidel sweep (solver_2d.py:670-692,
+//                   solver_3d.py:679-706); two launches make one sweep
+//   k_restrict      defect + red-point restriction onto level+1, also zeroes phi_{l+1}
+//                   (solver_2d.py:607-608, 616-647; solver_3d.py:613-614, 622-652)
+//   k_prolong       phi += P(phi_c) (solver_2d.py:612, 649-668; solver_3d.py:618, 654-677)
+// The coarse levels (few thousand points) run inside one thread block: k_coarse_cycle
+// executes the reference's recursion (solver_2d.py:582-614) from a given level down to
+// level L-2 with __syncthreads between operators, so a whole V/W/F sub-cycle is one launch.
+#include "mg_common.cuh"
+#include "mg_kernels.h"
+
+namespace jmg {
+
+// ------------------------------------------------------------------------------------
+// grid-wide operators
+// ------------------------------------------------------------------------------------
+
+// 2D: blockDim (64, 4); x walks the points of one colour in a row, y walks rows.
+template <typename T>
+__global__ void k_sweep_color2d(Lvl<T> a, int color) {
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  if (i > a.my) return;
+  const int j = 2 + ((i + color) & 1) + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (j > a.mx) return;
+  const long long p = (long long)i * a.P + j;
+  a.phi[p] = gs_point2d<T>(a.phi, a.rhs, a.wx, a.wy, a.invd, p, a.P);
+}
+
+// 3D: blockDim (64, 4, 1); grid z walks planes.
+template <typename T>
+__global__ void k_sweep_color3d(Lvl<T> a, int color) {
+  const int k = blockIdx.z + 2;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  if (j > a.my || k > a.mz) return;
+  // first colour in 3D: i+j+k odd (color 0); second: even
+  const int par = (first_color_parity<3>() + color) & 1;
+  const int i = 2 + ((j + k + par) & 1) + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (i > a.mx) return;
+  const long long p = (long long)k * a.S + (long long)j * a.P + i;
+  a.phi[p] = gs_point3d<T>(a.phi, a.rhs, a.wx, a.wy, a.wz, a.invd, p, a.P, a.S);
+}
+
+// Over the full padded coarse array: phi_c = 0, rhs_c = restricted defect inside, 0 on the frame.
+template <typename T>
+__global__ void k_restrict2d(Lvl<T> f, Lvl<T> c) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  if (I > c.mx + 2 || J > c.my + 2) return;
+  const long long q = (long long)J * c.P + I;
+  c.phi[q] = T(0);
+  T v = T(0);
+  if (J >= 2 && J <= c.my && I >= 2 && I <= c.mx) v = restrict_point2d<T>(f, J, I);
+  c.rhs[q] = v;
+}
+
+template <typename T>
+__global__ void k_restrict3d(Lvl<T> f, Lvl<T> c) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int K = blockIdx.z;
+  if (I > c.mx + 2 || J > c.my + 2) return;
+  const long long q = (long long)K * c.S + (long long)J * c.P + I;
+  c.phi[q] = T(0);
+  T v = T(0);
+  if (K >= 2 && K <= c.mz && J >= 2 && J <= c.my && I >= 2 && I <= c.mx) v = restrict_point3d<T>(f, K, J, I);
+  c.rhs[q] = v;
+}
+
+template <typename T>
+__global__ void k_prolong2d(Lvl<T> f, Lvl<T> c, int diag) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  if (i > f.my || j > f.mx) return;
+  T v;
+  if (prolong_point2d<T>(c, i, j, diag != 0, &v)) {
+    const long long p = (long long)i * f.P + j;
+    f.phi[p] = f.phi[p] + v;
+  }
+}
+
+template <typename T>
+__global__ void k_prolong3d(Lvl<T> f, Lvl<T> c, int bilinear) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int k = blockIdx.z + 2;
+  if (i > f.mx || j > f.my) return;
+  T v;
+  if (prolong_point3d<T>(c, k, j, i, bilinear != 0, &v)) {
+    const long long p = (long long)k * f.S + (long long)j * f.P + i;
+    f.phi[p] = f.phi[p] + v;
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// single-block coarse cycle
+// ------------------------------------------------------------------------------------
+
+template <typename T, int DIM>
+__device__ void blk_sweep(const Lvl<T>& a) {
+  const int nt = blockDim.x;
+  for (int color = 0; color < 2; ++color) {
+    if (DIM == 2) {
+      const int hx = a.mx / 2;  // points of one colour per row (m even) -- m >= 2
+      const int rows = a.my - 1;
+      const int n = hx * rows;
+      for (int t = threadIdx.x; t < n; t += nt) {
+        const int i = 2 + t / hx;
+        const int j = 2 + ((i + color) & 1) + 2 * (t % hx);
+        if (j > a.mx) continue;
+        const long long p = (long long)i * a.P + j;
+        a.phi[p] = gs_point2d<T>(a.phi, a.rhs, a.wx, a.wy, a.invd, p, a.P);
+      }
+    } else {
+      const int hx = a.mx / 2;
+      const int ny = a.my - 1, nz = a.mz - 1;
+      const int n = hx * ny * nz;
+      const int par = (first_color_parity<3>() + color) & 1;
+      for (int t = threadIdx.x; t < n; t += nt) {
+        const int r = t / hx;
+        const int j = 2 + r % ny, k = 2 + r / ny;
+        const int i = 2 + ((j + k + par) & 1) + 2 * (t % hx);
+        if (i > a.mx) continue;
+        const long long p = (long long)k * a.S + (long long)j * a.P + i;
+        a.phi[p] = gs_point3d<T>(a.phi, a.rhs, a.wx, a.wy, a.wz, a.invd, p, a.P, a.S);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int DIM>
+__device__ void blk_restrict(const Lvl<T>& f, const Lvl<T>& c) {
+  const int nx = c.mx + 3, ny = c.my + 3, nz = DIM == 3 ? c.mz + 3 : 1;
+  const int n = nx * ny * nz;
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    const int I = t % nx, J = (t / nx) % ny, K = t / (nx * ny);
+    const long long q = (long long)K * c.S + (long long)J * c.P + I;
+    T v = T(0);
+    if (DIM == 2) {
+      if (J >= 2 && J <= c.my && I >= 2 && I <= c.mx) v = restrict_point2d<T>(f, J, I);
+    } else {
+      if (K >= 2 && K <= c.mz && J >= 2 && J <= c.my && I >= 2 && I <= c.mx) v = restrict_point3d<T>(f, K, J, I);
+    }
+    c.rhs[q] = v;
+    c.phi[q] = T(0);
+  }
+  __syncthreads();
+}
+
+template <typename T, int DIM>
+__device__ void blk_prolong(const Lvl<T>& f, const Lvl<T>& c, bool diag) {
+  const int nx = f.mx - 1, ny = f.my - 1, nz = DIM == 3 ? f.mz - 1 : 1;
+  const int n = nx * ny * nz;
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    const int i = 2 + t % nx, j = 2 + (t / nx) % ny, k = 2 + t / (nx * ny);
+    T v;
+    bool ok = DIM == 2 ? prolong_point2d<T>(c, j, i, diag, &v) : prolong_point3d<T>(c, k, j, i, diag, &v);
+    if (ok) {
+      const long long p = DIM == 2 ? (long long)j * f.P + i : (long long)k * f.S + (long long)j * f.P + i;
+      f.phi[p] = f.phi[p] + v;
+    }
+  }
+  __syncthreads();
+}
+
+// multigrid_cycle (solver_2d.py:582-614) restricted to levels >= lev, run by one block.
+template <typename T, int DIM>
+__device__ void blk_cycle(const LvlTable<T>& tab, const CycleParams& cp, int lev, bool fcycle, bool skip_pre) {
+  if (lev == cp.last_level) {
+    for (int s = 0; s < cp.nu1 + cp.nu2; ++s) blk_sweep<T, DIM>(tab.l[lev]);
+    return;
+  }
+  if (!skip_pre)
+    for (int s = 0; s < cp.nu1; ++s) blk_sweep<T, DIM>(tab.l[lev]);
+  blk_restrict<T, DIM>(tab.l[lev], tab.l[lev + 1]);
+  if (fcycle)
+    for (int g = 0; g < cp.gamma; ++g) blk_cycle<T, DIM>(tab, cp, lev + 1, true, false);
+  for (int g = 0; g < cp.gamma; ++g) blk_cycle<T, DIM>(tab, cp, lev + 1, false, false);
+  blk_prolong<T, DIM>(tab.l[lev], tab.l[lev + 1], cp.diag != 0);
+  for (int s = 0; s < cp.nu2; ++s) blk_sweep<T, DIM>(tab.l[lev]);
+}
+
+template <typename T, int DIM>
+__global__ void __launch_bounds__(1024) k_coarse_cycle(LvlTable<T> tab, CycleParams cp, int lev, int fcycle,
+                                                      int skip_pre) {
+  blk_cycle<T, DIM>(tab, cp, lev, fcycle != 0, skip_pre != 0);
+}
+
+// ------------------------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------------------------
+
+static inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
+
+template <typename T>
+void launch_sweep(int dim, const Lvl<T>& a, cudaStream_t s) {
+  for (int color = 0; color < 2; ++color) {
+    if (dim == 2) {
+      dim3 b(64, 4), g(cdiv(a.mx / 2, 64), cdiv(a.my - 1, 4));
+      k_sweep_color2d<T><<<g, b, 0, s>>>(a, color);
+    } else {
+      dim3 b(64, 4, 1), g(cdiv(a.mx / 2, 64), cdiv(a.my - 1, 4), a.mz - 1);
+      k_sweep_color3d<T><<<g, b, 0, s>>>(a, color);
+    }
+  }
+}
+
+template <typename T>
+void launch_restrict(int dim, const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s) {
+  if (dim == 2) {
+    dim3 b(32, 8), g(cdiv(c.mx + 3, 32), cdiv(c.my + 3, 8));
+    k_restrict2d<T><<<g, b, 0, s>>>(f, c);
+  } else {
+    dim3 b(32, 8, 1), g(cdiv(c.mx + 3, 32), cdiv(c.my + 3, 8), c.mz + 3);
+    k_restrict3d<T><<<g, b, 0, s>>>(f, c);
+  }
+}
+
+template <typename T>
+void launch_prolong(int dim, const Lvl<T>& f, const Lvl<T>& c, int diag, cudaStream_t s) {
+  if (dim == 2) {
+    dim3 b(64, 4), g(cdiv(f.mx - 1, 64), cdiv(f.my - 1, 4));
+    k_prolong2d<T><<<g, b, 0, s>>>(f, c, diag);
+  } else {
+    dim3 b(64, 4, 1), g(cdiv(f.mx - 1, 64), cdiv(f.my - 1, 4), f.mz - 1);
+    k_prolong3d<T><<<g, b, 0, s>>>(f, c, diag);
+  }
+}
+
+template <typename T>
+void launch_coarse_cycle(int dim, const LvlTable<T>& tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
+                         cudaStream_t s) {
+  if (dim == 2)
+    k_coarse_cycle<T, 2><<<1, 1024, 0, s>>>(tab, cp, lev, fcycle, skip_pre);
+  else
+    k_coarse_cycle<T, 3><<<1, 1024, 0, s>>>(tab, cp, lev, fcycle, skip_pre);
+}
+
+#define JMG_INST(T)                                                                               \
+  template void launch_sweep<T>(int, const Lvl<T>&, cudaStream_t);                                \
+  template void launch_restrict<T>(int, const Lvl<T>&, const Lvl<T>&, cudaStream_t);              \
+  template void launch_prolong<T>(int, const Lvl<T>&, const Lvl<T>&, int, cudaStream_t);          \
+  template void launch_coarse_cycle<T>(int, const LvlTable<T>&, const CycleParams&, int, int, int, cudaStream_t);
+JMG_INST(double)
+JMG_INST(float)
+#undef JMG_INST
+
+}  // namespace jmg

@@ -1,0 +1,82 @@
+// mg_kernels.h — host-side launchers of the solver kernels (internal to libjmg).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mg_common.cuh"
+
+namespace jmg {
+
+struct CycleParams {
+  int last_level;  // L-2: the deepest level visited (solver_2d.py:601)
+  int nu1, nu2, gamma;
+  int diag;        // prolongate the (even,even) points in 2D / bilinear points in 3D
+};
+
+// Scalars the device loop keeps in the workspace.
+struct LoopState {
+  unsigned long long dist_bits;  // max |phi_old - phi| as ordered bits (abs_bits)
+  long long count;               // cycles done
+  double res_norm;               // current ||r||_2 (residual stop)
+  double rhs_norm;               // ||rhs||_2 over the interior (residual stop)
+  double rel_res;                // res_norm / rhs_norm
+  int go;                        // last loop decision
+  int pad;
+};
+
+template <typename T> void launch_sweep(int dim, const Lvl<T>& a, cudaStream_t s);
+template <typename T> void launch_restrict(int dim, const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s);
+template <typename T> void launch_prolong(int dim, const Lvl<T>& f, const Lvl<T>& c, int diag, cudaStream_t s);
+template <typename T>
+void launch_coarse_cycle(int dim, const LvlTable<T>& tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
+                         cudaStream_t s);
+
+// mg_aux.cu
+struct Box {  // padded extents of one level
+  int nx, ny, nz;  // m+3 per axis (nz = 1 in 2D)
+  int P;
+  long long S;
+};
+void launch_copy_in(const Box& b, const double* src_dense, double* dst, int zero_frame, cudaStream_t s);
+void launch_copy_out(const Box& b, const double* src, double* dst_dense, cudaStream_t s);
+void launch_do_bcs_dense(int dim, const int32_t* shape, double* arr, cudaStream_t s);
+// max |a - b| over the padded box into st->dist_bits (after zeroing it), then a <- b.
+void launch_distance_snapshot(const Box& b, double* old_phi, const double* phi, LoopState* st, cudaStream_t s);
+// partial sums of squares of the defect (or of rhs when phi == nullptr) over the interior
+template <typename T>
+void launch_residual_partials(int dim, const Lvl<T>& a, const T* phi_or_null, double* partials, int nparts,
+                              cudaStream_t s);
+int residual_num_parts(int dim, const Box& b);
+// device-side loop decisions
+void launch_loop_init(LoopState* st, const double* partials, int nparts, int mode, double rtol,
+                      long long max_iters, unsigned long long cond_handle, cudaStream_t s);
+void launch_loop_step(LoopState* st, const double* partials, int nparts, int mode, double eps, double rtol,
+                      long long max_iters, unsigned long long cond_handle, cudaStream_t s);
+void launch_rhs_norm(LoopState* st, const double* partials, int nparts, cudaStream_t s);
+void launch_rel_residual_out(const LoopState* st, const double* partials, int nparts, double* out, cudaStream_t s);
+void launch_count_out(const LoopState* st, long long* out, cudaStream_t s);
+void launch_dense_residual(int dim, const Lvl<double>& a, const Box& b, double* d_dense, cudaStream_t s);
+void launch_copy_coeff(const Box& b, const double* src, double* dst_dense, cudaStream_t s);
+
+// mixed precision helpers (mg_aux.cu)
+// r32 = rhs - L_h phi (FP64 arithmetic, FP32 result) on the interior, zero frame.
+void launch_residual_to_f32(int dim, const Lvl<double>& a, float* r32, cudaStream_t s);
+// phi += e32 on the interior; e32 untouched.
+void launch_add_correction(int dim, const Lvl<double>& a, const float* e32, cudaStream_t s);
+void launch_zero_f32(const Box& b, float* x, cudaStream_t s);
+void launch_convert_f32(const Box& b, const double* src, float* dst, cudaStream_t s);
+
+// mg_hierarchy.cu
+struct HierInputs {
+  const double* lam; double lam_scalar;
+  const double* D[3]; double D_scalar[3];
+  int scalar_D;     // all D components scalar
+  int scalar_lam;
+};
+// Builds wx, wy, (wz), acc, invd of level l (and the averaged D arrays of level l in 3D).
+// dprev: averaged D of level l-1 (3D, l >= 2), or nullptr.
+void launch_hierarchy_level(int dim, int level, const Lvl<double>& a, const Box& b, const Box& b0,
+                            const HierInputs& in, const double* sq_idel, double* const* d_cur,
+                            const double* const* d_prev, const Box& bprev, cudaStream_t s);
+
+}  // namespace jmg
