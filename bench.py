@@ -190,7 +190,7 @@ def main():
     p = workloads.random_2d(m, seed=args.seed + rank)
     g = grid_1D(m)
     kw = cycle_kw(args.cycle)
-    opts = dict(stop="residual", rtol=RTOL, precision=args.form, **kw)
+    opts = dict(stop="residual", rtol=RTOL, precision=args.form, max_iters_outer=20000, **kw)
     lib = _lib.load()
     cfg = _engine.make_config(**opts)
     plan = _lib.Plan(_engine.make_grid((g, g)), cfg)

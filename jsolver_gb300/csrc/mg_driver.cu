@@ -69,7 +69,7 @@ struct JmgPlan {
   int coarse_start = 0; // first level run by the single-block kernel
   bool mixed = false;
   std::vector<LevelInfo> lv;
-  size_t off_phi_old = 0, off_state = 0, off_parts = 0, ws_bytes = 0;
+  size_t off_phi_old = 0, off_state = 0, off_parts = 0, off_tab64 = 0, off_tab32 = 0, ws_bytes = 0;
   int nparts = 0;
   // graph cache
   cudaGraphExec_t exec = nullptr;
@@ -155,6 +155,8 @@ int validate_and_layout(JmgPlan* p) {
   p->off_state = take(sizeof(LoopState));
   p->nparts = residual_num_parts(d, p->lv[0].box);
   p->off_parts = take((size_t)p->nparts * 8 + 64);
+  p->off_tab64 = take(sizeof(LvlTable<double>));
+  p->off_tab32 = take(sizeof(LvlTable<float>));
   p->ws_bytes = off;
   // coarse levels: at most 8192 padded points, and never below the last visited level
   int cs = p->used - 1;
@@ -242,8 +244,8 @@ CycleParams cycle_params(const JmgPlan* p, bool off_diag) {
 // multigrid_cycle, solver_2d.py:582-614, emitted as launches on stream s. With a
 // non-null `count`, nothing is launched and the number of kernel launches is added.
 template <typename T>
-void emit_cycle(const JmgPlan* p, const LvlTable<T>& tab, const CycleParams& cp, int lev, bool fcycle,
-                bool skip_pre, cudaStream_t s, long long* count = nullptr) {
+void emit_cycle(const JmgPlan* p, const LvlTable<T>& tab, const LvlTable<T>* dtab, const CycleParams& cp, int lev,
+                bool fcycle, bool skip_pre, cudaStream_t s, long long* count = nullptr) {
   const int dim = p->dim;
   auto sweep = [&]() {
     if (count) *count += 2;
@@ -251,7 +253,7 @@ void emit_cycle(const JmgPlan* p, const LvlTable<T>& tab, const CycleParams& cp,
   };
   if (lev >= p->coarse_start) {
     if (count) *count += 1;
-    else launch_coarse_cycle<T>(dim, tab, cp, lev, fcycle ? 1 : 0, skip_pre ? 1 : 0, s);
+    else launch_coarse_cycle<T>(dim, dtab, cp, lev, fcycle ? 1 : 0, skip_pre ? 1 : 0, s);
     return;
   }
   if (lev == cp.last_level) {
@@ -263,8 +265,8 @@ void emit_cycle(const JmgPlan* p, const LvlTable<T>& tab, const CycleParams& cp,
   if (count) *count += 1;
   else launch_restrict<T>(dim, tab.l[lev], tab.l[lev + 1], s);
   if (fcycle)
-    for (int g = 0; g < cp.gamma; ++g) emit_cycle<T>(p, tab, cp, lev + 1, true, false, s, count);
-  for (int g = 0; g < cp.gamma; ++g) emit_cycle<T>(p, tab, cp, lev + 1, false, false, s, count);
+    for (int g = 0; g < cp.gamma; ++g) emit_cycle<T>(p, tab, dtab, cp, lev + 1, true, false, s, count);
+  for (int g = 0; g < cp.gamma; ++g) emit_cycle<T>(p, tab, dtab, cp, lev + 1, false, false, s, count);
   if (count) *count += 1;
   else launch_prolong<T>(dim, tab.l[lev], tab.l[lev + 1], cp.diag, s);
   for (int k = 0; k < cp.nu2; ++k) sweep();
@@ -284,7 +286,8 @@ void emit_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaStream
   CycleParams cp = cycle_params(p, false);
   if (!p->mixed) {
     LvlTable<double> tab = make_table<double>(p, ws);
-    emit_cycle<double>(p, tab, cp, 0, p->cfg.fcycle != 0, p->cfg.skip_pre != 0, s);
+    emit_cycle<double>(p, tab, ptr<LvlTable<double>>(ws, p->off_tab64), cp, 0, p->cfg.fcycle != 0,
+                       p->cfg.skip_pre != 0, s);
   } else {
     // FP64 iterative refinement around FP32 cycles: r = rhs - L_h phi (FP64), solve
     // L_h e = r with FP32 cycles from e = 0, phi += e (FP64)
@@ -292,7 +295,8 @@ void emit_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaStream
     launch_residual_to_f32(p->dim, l0, t32.l[0].rhs, s);
     launch_zero_f32(p->lv[0].box, t32.l[0].phi, s);
     const int inner = p->cfg.inner_cycles > 0 ? p->cfg.inner_cycles : 1;
-    for (int k = 0; k < inner; ++k) emit_cycle<float>(p, t32, cp, 0, p->cfg.fcycle != 0, false, s);
+    for (int k = 0; k < inner; ++k)
+      emit_cycle<float>(p, t32, ptr<LvlTable<float>>(ws, p->off_tab32), cp, 0, p->cfg.fcycle != 0, false, s);
     launch_add_correction(p->dim, l0, t32.l[0].phi, s);
   }
   if (mode == 0) launch_distance_snapshot(p->lv[0].box, ptr<double>(ws, p->off_phi_old), l0.phi, st, s);
@@ -306,12 +310,12 @@ long long body_launches(const JmgPlan* p) {
   if (!p->mixed) {
     LvlTable<double> t;
     memset(&t, 0, sizeof(t));
-    emit_cycle<double>(p, t, cp, 0, p->cfg.fcycle != 0, p->cfg.skip_pre != 0, nullptr, &n);
+    emit_cycle<double>(p, t, nullptr, cp, 0, p->cfg.fcycle != 0, p->cfg.skip_pre != 0, nullptr, &n);
   } else {
     LvlTable<float> t;
     memset(&t, 0, sizeof(t));
     const int inner = p->cfg.inner_cycles > 0 ? p->cfg.inner_cycles : 1;
-    for (int k = 0; k < inner; ++k) emit_cycle<float>(p, t, cp, 0, p->cfg.fcycle != 0, false, nullptr, &n);
+    for (int k = 0; k < inner; ++k) emit_cycle<float>(p, t, nullptr, cp, 0, p->cfg.fcycle != 0, false, nullptr, &n);
     n += 3;  // residual_to_f32, zero, add_correction
   }
   const int mode = loop_mode(p);
@@ -520,8 +524,10 @@ int jmg_solve(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs
   launch_copy_in(b0, phi0, l0.phi, 1, s);
   launch_copy_in(b0, phi0, phi_old, 0, s);
   launch_copy_in(b0, rhs, l0.rhs, 1, s);
-  // 2. coefficients
+  // 2. coefficients, and the level tables the single-block coarse kernel reads
   if ((rc = build_hierarchy(p, c, ws, s))) return rc;
+  launch_store_table<double>(make_table<double>(p, ws), ptr<LvlTable<double>>(ws, p->off_tab64), s);
+  if (p->mixed) launch_store_table<float>(make_table<float>(p, ws), ptr<LvlTable<float>>(ws, p->off_tab32), s);
   if (mode == 1) {
     launch_residual_partials<double>(p->dim, l0, nullptr, parts, p->nparts, s);
     launch_rhs_norm(st, parts, p->nparts, s);
@@ -688,7 +694,7 @@ int jmg_plan_launch_counts(const JmgPlan* p, int64_t* per_solve_fixed, int64_t* 
   if (!p) return set_err(JMG_ERR_VALUE, "plan must not be NULL");
   // copy-ins (3), hierarchy (2 per level + FP32 conversions), rhs norm (2), loop init
   // (1-2), copy-out and count (2)
-  long long fixed = 3 + 2LL * p->used + 2 + 2;
+  long long fixed = 3 + 2LL * p->used + 2 + 2 + (p->mixed ? 2 : 1);
   if (p->mixed) fixed += (long long)p->used * (p->dim == 3 ? 5 : 4);
   if (loop_mode(p) == 1) fixed += 2 + 1;
   fixed += 1;

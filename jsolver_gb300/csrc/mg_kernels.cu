@@ -167,26 +167,69 @@ __device__ void blk_prolong(const Lvl<T>& f, const Lvl<T>& c, bool diag) {
 }
 
 // multigrid_cycle (solver_2d.py:582-614) restricted to levels >= lev, run by one block.
+// The recursion is unrolled into an explicit stack of frames (no device recursion, so the
+// per-thread stack stays within its default size). Every thread walks the same frames,
+// so the __syncthreads inside the operators are reached uniformly.
 template <typename T, int DIM>
-__device__ void blk_cycle(const LvlTable<T>& tab, const CycleParams& cp, int lev, bool fcycle, bool skip_pre) {
-  if (lev == cp.last_level) {
-    for (int s = 0; s < cp.nu1 + cp.nu2; ++s) blk_sweep<T, DIM>(tab.l[lev]);
-    return;
+__device__ void blk_cycle(const LvlTable<T>* __restrict__ tab, const CycleParams& cp, int lev0, bool fcycle0,
+                          bool skip_pre0) {
+  struct Frame {
+    int lev, stage, g;
+    bool fcycle, skip_pre;
+  };
+  Frame st[kMaxLevels + 1];
+  int sp = 0;
+  st[sp++] = Frame{lev0, 0, 0, fcycle0, skip_pre0};
+  while (sp > 0) {
+    Frame& f = st[sp - 1];
+    const Lvl<T> a = tab->l[f.lev];
+    if (f.lev == cp.last_level) {
+      for (int s = 0; s < cp.nu1 + cp.nu2; ++s) blk_sweep<T, DIM>(a);
+      --sp;
+      continue;
+    }
+    if (f.stage == 0) {
+      if (!f.skip_pre)
+        for (int s = 0; s < cp.nu1; ++s) blk_sweep<T, DIM>(a);
+      blk_restrict<T, DIM>(a, tab->l[f.lev + 1]);
+      f.stage = f.fcycle ? 1 : 2;
+      f.g = 0;
+    }
+    if (f.stage == 1) {  // F-cycle: gamma recursive F-cycles first (solver_2d.py:609-610)
+      if (f.g < cp.gamma) {
+        ++f.g;
+        st[sp++] = Frame{f.lev + 1, 0, 0, true, false};
+        continue;
+      }
+      f.stage = 2;
+      f.g = 0;
+    }
+    if (f.stage == 2) {  // gamma plain cycles (solver_2d.py:611)
+      if (f.g < cp.gamma) {
+        ++f.g;
+        st[sp++] = Frame{f.lev + 1, 0, 0, false, false};
+        continue;
+      }
+      f.stage = 3;
+    }
+    blk_prolong<T, DIM>(a, tab->l[f.lev + 1], cp.diag != 0);
+    for (int s = 0; s < cp.nu2; ++s) blk_sweep<T, DIM>(a);
+    --sp;
   }
-  if (!skip_pre)
-    for (int s = 0; s < cp.nu1; ++s) blk_sweep<T, DIM>(tab.l[lev]);
-  blk_restrict<T, DIM>(tab.l[lev], tab.l[lev + 1]);
-  if (fcycle)
-    for (int g = 0; g < cp.gamma; ++g) blk_cycle<T, DIM>(tab, cp, lev + 1, true, false);
-  for (int g = 0; g < cp.gamma; ++g) blk_cycle<T, DIM>(tab, cp, lev + 1, false, false);
-  blk_prolong<T, DIM>(tab.l[lev], tab.l[lev + 1], cp.diag != 0);
-  for (int s = 0; s < cp.nu2; ++s) blk_sweep<T, DIM>(tab.l[lev]);
 }
 
 template <typename T, int DIM>
-__global__ void __launch_bounds__(1024) k_coarse_cycle(LvlTable<T> tab, CycleParams cp, int lev, int fcycle,
+__global__ void __launch_bounds__(1024) k_coarse_cycle(const LvlTable<T>* tab, CycleParams cp, int lev, int fcycle,
                                                       int skip_pre) {
   blk_cycle<T, DIM>(tab, cp, lev, fcycle != 0, skip_pre != 0);
+}
+
+template <typename T>
+__global__ void k_store_table(LvlTable<T> tab, LvlTable<T>* dst) {
+  const int n = sizeof(LvlTable<T>) / sizeof(int);
+  const int* src = reinterpret_cast<const int*>(&tab);
+  int* d = reinterpret_cast<int*>(dst);
+  for (int k = threadIdx.x; k < n; k += blockDim.x) d[k] = src[k];
 }
 
 // ------------------------------------------------------------------------------------
@@ -231,7 +274,7 @@ void launch_prolong(int dim, const Lvl<T>& f, const Lvl<T>& c, int diag, cudaStr
 }
 
 template <typename T>
-void launch_coarse_cycle(int dim, const LvlTable<T>& tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
+void launch_coarse_cycle(int dim, const LvlTable<T>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
                          cudaStream_t s) {
   if (dim == 2)
     k_coarse_cycle<T, 2><<<1, 1024, 0, s>>>(tab, cp, lev, fcycle, skip_pre);
@@ -239,11 +282,17 @@ void launch_coarse_cycle(int dim, const LvlTable<T>& tab, const CycleParams& cp,
     k_coarse_cycle<T, 3><<<1, 1024, 0, s>>>(tab, cp, lev, fcycle, skip_pre);
 }
 
+template <typename T>
+void launch_store_table(const LvlTable<T>& tab, LvlTable<T>* dst, cudaStream_t s) {
+  k_store_table<T><<<1, 128, 0, s>>>(tab, dst);
+}
+
 #define JMG_INST(T)                                                                               \
   template void launch_sweep<T>(int, const Lvl<T>&, cudaStream_t);                                \
   template void launch_restrict<T>(int, const Lvl<T>&, const Lvl<T>&, cudaStream_t);              \
   template void launch_prolong<T>(int, const Lvl<T>&, const Lvl<T>&, int, cudaStream_t);          \
-  template void launch_coarse_cycle<T>(int, const LvlTable<T>&, const CycleParams&, int, int, int, cudaStream_t);
+  template void launch_coarse_cycle<T>(int, const LvlTable<T>*, const CycleParams&, int, int, int, cudaStream_t); \
+  template void launch_store_table<T>(const LvlTable<T>&, LvlTable<T>*, cudaStream_t);
 JMG_INST(double)
 JMG_INST(float)
 #undef JMG_INST

@@ -28,8 +28,10 @@ template <typename T> void launch_sweep(int dim, const Lvl<T>& a, cudaStream_t s
 template <typename T> void launch_restrict(int dim, const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s);
 template <typename T> void launch_prolong(int dim, const Lvl<T>& f, const Lvl<T>& c, int diag, cudaStream_t s);
 template <typename T>
-void launch_coarse_cycle(int dim, const LvlTable<T>& tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
+void launch_coarse_cycle(int dim, const LvlTable<T>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
                          cudaStream_t s);
+// copies a level table into device memory (the coarse kernel reads it from there)
+template <typename T> void launch_store_table(const LvlTable<T>& tab, LvlTable<T>* dst, cudaStream_t s);
 
 // mg_aux.cu
 struct Box {  // padded extents of one level
