@@ -159,6 +159,21 @@ int jmg_op_smooth_ws(JmgPlan* plan, int level, int nsweeps, void* workspace, siz
  * counterpart: it reports this library's launch schedule. */
 int jmg_plan_launch_counts(const JmgPlan* plan, int64_t* per_solve_fixed, int64_t* per_cycle);
 
+/* Relative residual ||rhs - L_h phi||_2 / ||rhs||_2 over interior indices 2..m, FP64,
+ * written to the device double *out, for callers that cannot allocate device memory
+ * (a server that owns the whole device heap in its own pool, a plugin host that passes
+ * only inputs and outputs, a loop that cannot afford an allocation's synchronisation).
+ * No counterpart in the reference. It needs no plan and no workspace: its scratch is a
+ * fixed 16 MiB array of this library's device memory, kept on every GPU that loads the
+ * library until the process exits, so grids whose level-0 coefficients need more
+ * (roughly 2D beyond 512^2, 3D beyond 64^3) are rejected with JMG_ERR_VALUE. The first
+ * call on each device looks up the array's address; make it outside stream capture.
+ * All calls share the array: calls that overlap on the GPU race, so serialise them.
+ * phi, rhs and the coefficient arrays are dense padded device arrays, as for jmg_solve;
+ * phi's frame is used as stored (the solver returns phi with a zero frame). */
+int jmg_rel_residual_noalloc(const JmgGrid* grid, const double* phi, const double* rhs,
+                             const JmgCoeffs* coeffs, double* out, jmg_stream_t stream);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* jmg_last_error(void);
 

@@ -450,6 +450,8 @@ __global__ void k_write_i64(long long* out, long long v) { *out = v; }
 
 }  // namespace
 
+int jmg::set_error_message(int code, const char* msg) { return set_err(code, "%s", msg); }
+
 // ---------------------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------------------

@@ -68,6 +68,9 @@ void launch_add_correction(int dim, const Lvl<double>& a, const float* e32, cuda
 void launch_zero_f32(const Box& b, float* x, cudaStream_t s);
 void launch_convert_f32(const Box& b, const double* src, float* dst, cudaStream_t s);
 
+// mg_driver.cu: records the message jmg_last_error() returns; returns code
+int set_error_message(int code, const char* msg);
+
 // mg_hierarchy.cu
 struct HierInputs {
   const double* lam; double lam_scalar;
