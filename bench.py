@@ -29,23 +29,45 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "ms to rel. residual 1e-10 (2D 1024^2 random-coefficient problem)"
 RTOL = 1e-10
-M = 1024
+WORKLOADS = {  # name -> (dimension, default resolution, default cycle)
+    "2d": (2, 1024, "V"),  # 2D 1024^2 random-coefficient problem (arrays 1027^2 float64)
+    "3d": (3, 256, "F"),   # 3D 256^3 random-coefficient problem (arrays 259^3 float64)
+}
+
+
+def metric_name(dim, m):
+    return f"ms to rel. residual 1e-10 ({dim}D {m}^{dim} random-coefficient problem)"
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--cycle", default="V", choices=["V", "W", "F"])
-    ap.add_argument("--m", type=int, default=M)
+    ap.add_argument("--workload", default="2d", choices=sorted(WORKLOADS))
+    ap.add_argument("--cycle", default=None, choices=["V", "W", "F"])
+    ap.add_argument("--m", type=int, default=None)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--no-e2e", action="store_true")
+    a = ap.parse_args()
+    dim, m, cyc = WORKLOADS[a.workload]
+    a.dim = dim
+    a.m = a.m or m
+    a.cycle = a.cycle or cyc
+    return a
+
+
+def make_problem(args, seed):
+    from jsolver_gb300 import workloads
+    return workloads.random_2d(args.m, seed=seed) if args.dim == 2 else workloads.random_3d(args.m, seed=seed)
+
+
+def coeff_names(dim):
+    return ["D_xx", "D_yy"] if dim == 2 else ["D_xx", "D_yy", "D_zz"]
 
 
 def cycle_kw(c):
@@ -73,7 +95,7 @@ class Clocks:
     def __enter__(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.p = None
@@ -114,29 +136,29 @@ def reference_arm(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    from jsolver_gb300 import workloads
     from oracle import c_oracle
     from oracle.grid import OracleGrid1D
-    p = workloads.random_2d(args.m, seed=args.seed)
+    p = make_problem(args, args.seed)
     g = OracleGrid1D(args.m)
     nthreads = os.cpu_count() or 1
     times, counts = [], []
     kw = cycle_kw(args.cycle)
     for it in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        phi, cnt, rr = c_oracle.solve((g, g), p["phi0"], p["rhs"], p["lam"], (p["D_xx"], p["D_yy"]), stop="residual",
-                                      rtol=RTOL, nthreads=nthreads, **kw)
+        phi, cnt, rr = c_oracle.solve((g,) * args.dim, p["phi0"], p["rhs"], p["lam"],
+                                      tuple(p[k] for k in coeff_names(args.dim)), stop="residual", rtol=RTOL,
+                                      nthreads=nthreads, **kw)
         dt = (time.perf_counter() - t0) * 1e3
         if it >= args.warmup:
             times.append(dt)
             counts.append(cnt)
     ms = float(np.median(times))
     line = {
-        "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded GRF coefficients, manufactured rhs)",
-        "impl": "reference",
-        "config": {"workload": f"2d-{args.m}x{args.m}-random-coeff (arrays {args.m + 3}^2 float64)",
+        "metric": metric_name(args.dim, args.m), "value": ms, "unit": "ms", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded GRF coefficients, manufactured rhs)", "impl": "reference",
+        "config": {"workload": workload_name(args),
                    "cycle": args.cycle, "stop": f"rel. residual <= {RTOL}", "cycles": counts[-1]},
         "cpu_baseline": {"value": ms, "unit": "ms", "cores": nthreads, "kind": "port",
                          "sample": f"{args.steps} full solves (median), C/OpenMP restatement of the reference "
@@ -148,13 +170,18 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline(p, m, cycles_needed, kw, budget_s=20.0):
+def workload_name(args):
+    shape = "^".join([str(args.m + 3), str(args.dim)])
+    return f"{args.dim}d-{args.m}^{args.dim}-random-coeff (arrays {shape} float64)"
+
+
+def cpu_baseline(p, dim, m, cycles_needed, kw, budget_s=20.0):
     """Time the C oracle on the host cores: a bounded number of cycles, scaled to a solve."""
     from oracle import c_oracle
     from oracle.grid import OracleGrid1D
     g = OracleGrid1D(m)
     nthreads = os.cpu_count() or 1
-    args = ((g, g), p["phi0"], p["rhs"], p["lam"], (p["D_xx"], p["D_yy"]))
+    args = ((g,) * dim, p["phi0"], p["rhs"], p["lam"], tuple(p[k] for k in coeff_names(dim)))
     t0 = time.perf_counter()
     c_oracle.solve(*args, fixed=True, max_iters_outer=1, nthreads=nthreads, **kw)
     t1 = time.perf_counter() - t0
@@ -182,27 +209,29 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    from jsolver_gb300 import _engine, _lib, workloads
+    from jsolver_gb300 import _engine, _lib
     from jsolver_gb300.grid_1d import grid_1D
     from jsolver_gb300.solver_2d import solve_2d
+    from jsolver_gb300.solver_3d import solve_3d
 
-    m = args.m
-    p = workloads.random_2d(m, seed=args.seed + rank)
+    m, dim = args.m, args.dim
+    cn = coeff_names(dim)
+    p = make_problem(args, args.seed + rank)
     g = grid_1D(m)
     kw = cycle_kw(args.cycle)
     opts = dict(stop="residual", rtol=RTOL, precision=args.form, max_iters_outer=20000, **kw)
     lib = _lib.load()
     cfg = _engine.make_config(**opts)
-    plan = _lib.Plan(_engine.make_grid((g, g)), cfg)
+    plan = _lib.Plan(_engine.make_grid((g,) * dim), cfg)
     stream = torch.cuda.Stream(dev)
-    d = {k: torch.from_numpy(p[k]).to(dev) for k in ("phi0", "rhs", "lam", "D_xx", "D_yy")}
+    d = {k: torch.from_numpy(p[k]).to(dev) for k in ["phi0", "rhs", "lam"] + cn}
     out = torch.empty_like(d["phi0"])
     count = torch.zeros((), dtype=torch.int64, device=dev)
     wsb = torch.empty(plan.workspace_bytes, dtype=torch.uint8, device=dev)
     coeffs = _lib.JmgCoeffs()
     coeffs.lam = d["lam"].data_ptr()
-    coeffs.D[0] = d["D_xx"].data_ptr()
-    coeffs.D[1] = d["D_yy"].data_ptr()
+    for k, name in enumerate(cn):
+        coeffs.D[k] = d[name].data_ptr()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     vp = ctypes.c_void_p
 
@@ -245,28 +274,31 @@ def main():
                                         vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()), vp(stream.cuda_stream)))
         stream.synchronize()
         rel_res = float(rr_t.item())
-        err_exact = float(np.abs(out.cpu().numpy() - p["phi_exact"]).max())
+        err_exact = (float(np.abs(out.cpu().numpy() - p["phi_exact"]).max()) if "phi_exact" in p else None)
 
-        # dominant kernel: fine-level red-black sweep, timed alone (2 colour launches/sweep)
-        nsw = 50
-        _lib.check(lib.jmg_op_smooth_ws(plan.handle, 0, 5, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()),
+        # dominant kernel: the fine-level FP64 red-black sweep (two colour launches), timed
+        # alone with CUDA events on its stream, L2 flushed before every sweep
+        nsw = 20
+        _lib.check(lib.jmg_op_smooth_ws(plan.handle, 0, 3, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()),
                                         vp(stream.cuda_stream)))
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        flush.zero_()
-        e0.record(stream)
-        _lib.check(lib.jmg_op_smooth_ws(plan.handle, 0, nsw, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()),
-                                        vp(stream.cuda_stream)))
-        e1.record(stream)
+        sw = []
+        for _ in range(nsw):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _lib.check(lib.jmg_op_smooth_ws(plan.handle, 0, 1, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()),
+                                            vp(stream.cuda_stream)))
+            e1.record(stream)
+            sw.append((e0, e1))
         stream.synchronize()
-        sweep_ms = e0.elapsed_time(e1) / nsw
-        n0 = (m + 3) ** 2
-        s_bytes = 8 if args.form == "fp64" else 4
-        alg_bytes_sweep = (2 + 4) * 8 * n0  # (d+4)*s*N0, d = 2, FP64 fine-level smoother
+        sweep_ms = float(np.mean([a.elapsed_time(b) for a, b in sw]))
+        n0 = (m + 3) ** dim
+        alg_bytes_sweep = (dim + 4) * 8 * n0  # (d+4)*s*N0: phi, rhs, d faces, 1/A_cc read; phi written
         launch_ms = sweep_ms / 2
-        achieved = alg_bytes_sweep / 2 / (launch_ms * 1e-3) / 1e9
+        achieved = alg_bytes_sweep / (sweep_ms * 1e-3) / 1e9
 
         # end to end through the public API from pinned host buffers
-        host = {k: torch.from_numpy(p[k]).pin_memory() for k in ("phi0", "rhs", "lam", "D_xx", "D_yy")}
+        host = {k: torch.from_numpy(p[k]).pin_memory() for k in ["phi0", "rhs", "lam"] + cn}
         dst = {k: torch.empty_like(d[k]) for k in host}
         phi_host = torch.empty(out.shape, dtype=torch.float64).pin_memory()
         cnt_host = torch.empty((), dtype=torch.int64).pin_memory()
@@ -274,15 +306,16 @@ def main():
         def e2e_step():
             for k in host:
                 dst[k].copy_(host[k], non_blocking=True)
-            phi, cnt = solve_2d(g, g, dst["phi0"], dst["rhs"], dst["lam"], dst["D_xx"], dst["D_yy"], **opts)
+            solve = solve_2d if dim == 2 else solve_3d
+            phi, cnt = solve(*((g,) * dim), dst["phi0"], dst["rhs"], dst["lam"], *[dst[k] for k in cn], **opts)
             phi_host.copy_(phi, non_blocking=True)
             cnt_host.copy_(cnt, non_blocking=True)
 
-        for _ in range(2):
+        for _ in range(0 if args.no_e2e else 2):
             e2e_step()
         stream.synchronize()
         e2e_t = []
-        for _ in range(args.steps):
+        for _ in range(0 if args.no_e2e else args.steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
@@ -290,7 +323,7 @@ def main():
             e1.record(stream)
             e1.synchronize()
             e2e_t.append(e0.elapsed_time(e1))
-        e2e_ms = float(np.mean(e2e_t))
+        e2e_ms = float(np.mean(e2e_t)) if e2e_t else None
         h2d = sum(t.numel() * 8 for t in host.values())
         d2h = phi_host.numel() * 8 + 8
 
@@ -309,32 +342,33 @@ def main():
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get("k_sweep_color2d_fp64_1024")
+            traffic = json.load(f).get(f"sweep_fp64_{dim}d_{m}")
     except (OSError, ValueError):
         pass
 
     line = {
-        "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": ws_n, "steps": args.steps, "warmup": args.warmup,
+        "metric": metric_name(dim, m), "value": ms, "unit": "ms", "n_gpus": ws_n, "steps": args.steps,
+        "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.form == "fp64" else "f32+f64",
         "data": "synthetic (seeded GRF coefficients, manufactured rhs; no dataset in the reference)",
-        "config": {"workload": f"2d-{m}x{m}-random-coeff (arrays {m + 3}^2 float64)", "cycle": args.cycle,
+        "config": {"workload": workload_name(args), "cycle": args.cycle,
                    "form": args.form, "stop": f"rel. residual <= {RTOL}", "cycles": cycles,
                    "l2": "flushed (256 MB write) before every timed solve", "parallelism": f"replicas x{ws_n}"},
         "solves_per_s": 1e3 / ms * ws_n,
         "final_rel_residual": rel_res,
         "max_err_vs_exact_discrete": err_exact,
-        "roofline": {"bound": "hbm", "kernel": "k_sweep_color2d<double> (fine level, one colour)",
+        "roofline": {"bound": "hbm", "kernel": f"k_sweep_color{dim}d<double> (fine level; 2 launches per sweep)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_src,
-                     "alg_bytes_per_launch": alg_bytes_sweep / 2, "launch_ms": launch_ms,
-                     "traffic": traffic},
-        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                     "peak_source": peak_src, "alg_bytes_per_sweep": alg_bytes_sweep,
+                     "alg_bytes_per_launch": alg_bytes_sweep / 2, "launch_ms": launch_ms, "traffic": traffic},
+        "e2e": ({"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+                if e2e_ms is not None else None),
         "gpu_launches": int(launches),
     }
     line["clocks"] = clk.summary()
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(p, m, cycles, kw)
+        line["cpu_baseline"] = cpu_baseline(p, dim, m, cycles, kw)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws_n > 1:

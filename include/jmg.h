@@ -148,6 +148,19 @@ int jmg_rel_residual(JmgPlan* plan, const double* phi, const double* rhs, double
  * boundary_handler_3d.py:3-35), in place on a dense padded device array. */
 int jmg_do_bcs(int ndim, const int32_t* shape, double* arr, jmg_stream_t stream);
 
+/* Reverse mode of the fixed-mode 2D solve: given phi_bar = dL/dphi_n for phi_n =
+ * solve_2d(..., fixed=True, max_iters_outer=n), writes the vector-Jacobian products
+ * dL/dphi0, dL/drhs, dL/dlam, dL/dD_xx, dL/dD_yy (dense padded arrays). Replaces
+ * jax.vjp of the reference's fixed mode (solver_2d.py:18-26, 461-463; exercised in
+ * tests/test_solver_2d.py:200-207). lam and D must be arrays. Needs the plan's workspace
+ * and an adjoint workspace of jmg_adjoint_workspace_bytes(plan) bytes (per-cycle
+ * checkpoints of phi plus per-operator snapshots of one cycle, which is recomputed). */
+size_t jmg_adjoint_workspace_bytes(const JmgPlan* plan);
+int jmg_solve_fixed_vjp(JmgPlan* plan, const double* phi0, const double* rhs, const JmgCoeffs* coeffs,
+                        const double* phi_bar, double* phi0_bar, double* rhs_bar, double* lam_bar,
+                        double* Dxx_bar, double* Dyy_bar, void* workspace, size_t workspace_bytes,
+                        void* adjoint_workspace, size_t adjoint_workspace_bytes, jmg_stream_t stream);
+
 /* Runs nsweeps red-black sweeps in place on the level arrays already in the workspace
  * (phi and rhs of that level as left by jmg_solve / jmg_op_*): the smoother of
  * red_black_gauss_seidel (solver_2d.py:670-692) without copies, for timing it alone. */

@@ -165,6 +165,16 @@ def solve(grids, phi, rhs, lam, D, D_xy=None, **opts):
     if off:
         raise NotImplementedError("spatially varying D with D_xy (9-point stencil) is not implemented on the GPU yet")
     torch_in = any(is_cuda_tensor(a) for a in [phi, rhs, lam] + list(D))
+    wants_grad = torch.is_grad_enabled() and any(isinstance(a, torch.Tensor) and a.requires_grad
+                                                 for a in [phi, rhs, lam] + list(D))
+    if wants_grad:
+        if not cfg.fixed:
+            raise ValueError("reverse-mode differentiation needs fixed=True, as in the reference "
+                             "(its dynamic while_loop is not reverse-differentiable)")
+        if ndim != 2 or cfg.precision != _lib.PREC_FP64:
+            raise NotImplementedError("the hand-written adjoint covers the 2D FP64 fixed-mode solve")
+        from .adjoint import solve_2d_fixed_diff
+        return solve_2d_fixed_diff(grids, phi, rhs, lam, D[0], D[1], **opts)
     device = pick_device(phi, rhs, lam, *D)
     _lib.load()
     with torch.cuda.device(device):

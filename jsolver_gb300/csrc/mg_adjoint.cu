@@ -1,0 +1,253 @@
+// mg_adjoint.cu — hand-written reverse mode of the fixed-mode 2D solve (vector-Jacobian
+// product), with per-cycle checkpointing and recomputation.
+//
+// The reference's fixed mode (solver_2d.py:461-463) is differentiated with jax.vjp, which
+// tapes every cycle (memory grows with cycles x grid, performance.md:44-60). Here:
+//   forward:  phi_0 (do_BCs) -> n cycles, keeping only phi at the start of every cycle;
+//   backward: for k = n-1 .. 0: re-run cycle k from its checkpoint with per-operator
+//             snapshots of phi, then apply the transposed operators in reverse order
+//             (mg_adjoint_kernels.cu): colour updates reversed, restriction <-> prolongation
+//             transposed; finally the backward of the coefficient hierarchy.
+// Outputs: adjoints of phi0, rhs, lambda, D_xx, D_yy (dense arrays, like the inputs). The
+// frame of phi is reset by do_BCs at every sweep and cycle, so its adjoint there is zero.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+#include "../../include/jmg.h"
+#include "mg_kernels.h"
+#include "mg_plan.h"
+
+namespace jmg {
+
+struct AdjLvl {
+  double *pb, *rb, *T, *gacc, *gwx, *gwy;
+};
+void adj_sweep(const Lvl<double>& a, const AdjLvl& g, const double* before, const double* after, cudaStream_t s);
+void adj_restrict(const Lvl<double>& a, const AdjLvl& g, const double* phi, const Lvl<double>& c, const AdjLvl& gc,
+                  cudaStream_t s);
+void adj_prolong(const Lvl<double>& f, const AdjLvl& gf, const Lvl<double>& c, const AdjLvl& gc, int diag,
+                 cudaStream_t s);
+void adj_hierarchy2d(const Lvl<double>& a, const AdjLvl& g, int level, double sx, double sy, int nx0, double* dbx,
+                     double* dby, double* dlam, cudaStream_t s);
+int set_error_message(int code, const char* msg);
+
+namespace {
+
+enum { OP_SWEEP = 0, OP_RESTRICT = 1, OP_PROLONG = 2 };
+constexpr int kZeros = -1;  // phi of a coarse level right after the restriction zeroed it
+constexpr int kInput = -2;  // phi of level 0 at the start of the cycle (the checkpoint)
+
+struct TapeOp {
+  int kind, lev, before, after;
+};
+
+struct Tape {
+  std::vector<TapeOp> ops;
+  std::vector<int> snap_lev;  // level of every snapshot
+};
+
+// the forward schedule of one cycle (solver_2d.py:582-614), with the phi state each
+// operator reads (before) and writes (after) as snapshot indices
+void tape_cycle(const JmgPlan* p, Tape& t, std::vector<int>& cur, int lev, bool fcycle, bool skip_pre) {
+  const CycleParams cp = cycle_params(p, false);
+  auto sweep = [&]() {
+    const int after = (int)t.snap_lev.size();
+    t.snap_lev.push_back(lev);
+    t.ops.push_back({OP_SWEEP, lev, cur[lev], after});
+    cur[lev] = after;
+  };
+  if (lev == cp.last_level) {
+    for (int k = 0; k < cp.nu1 + cp.nu2; ++k) sweep();
+    return;
+  }
+  if (!skip_pre)
+    for (int k = 0; k < cp.nu1; ++k) sweep();
+  t.ops.push_back({OP_RESTRICT, lev, cur[lev], -3});
+  cur[lev + 1] = kZeros;
+  if (fcycle)
+    for (int g = 0; g < cp.gamma; ++g) tape_cycle(p, t, cur, lev + 1, true, false);
+  for (int g = 0; g < cp.gamma; ++g) tape_cycle(p, t, cur, lev + 1, false, false);
+  const int after = (int)t.snap_lev.size();
+  t.snap_lev.push_back(lev);
+  t.ops.push_back({OP_PROLONG, lev, cur[lev], after});
+  cur[lev] = after;
+  for (int k = 0; k < cp.nu2; ++k) sweep();
+}
+
+Tape make_tape(const JmgPlan* p) {
+  Tape t;
+  std::vector<int> cur(p->used, kZeros);
+  cur[0] = kInput;
+  tape_cycle(p, t, cur, 0, p->cfg.fcycle != 0, p->cfg.skip_pre != 0);
+  return t;
+}
+
+struct AdjLayout {
+  size_t total = 0;
+  std::vector<size_t> lvl;   // 6 arrays per level
+  std::vector<size_t> snap;  // one level array per snapshot
+  size_t ckpt = 0;           // (n + 1) level-0 arrays
+  size_t zeros = 0;          // one level-0 array of zeros
+  size_t pre = 0;            // skip_pre: phi after each initial sweep (nu1 level-0 arrays)
+  int ncyc = 0;
+};
+
+AdjLayout adj_layout(const JmgPlan* p, const Tape& t) {
+  AdjLayout L;
+  size_t off = 0;
+  auto take = [&](size_t b) {
+    const size_t o = off;
+    off = align_up(off + b);
+    return o;
+  };
+  for (int l = 0; l < p->used; ++l) L.lvl.push_back(take(6 * p->lv[l].elems * 8));
+  for (int lev : t.snap_lev) L.snap.push_back(take(p->lv[lev].elems * 8));
+  L.ncyc = p->cfg.max_iters_outer > 0 ? (int)p->cfg.max_iters_outer : 0;
+  L.ckpt = take((size_t)(L.ncyc + 1) * p->lv[0].elems * 8);
+  L.zeros = take(p->lv[0].elems * 8);
+  const int nu1 = p->cfg.nu1 > 0 ? p->cfg.nu1 : 0;
+  L.pre = take((size_t)(p->cfg.skip_pre ? nu1 + 1 : 1) * p->lv[0].elems * 8);
+  L.total = off;
+  return L;
+}
+
+AdjLvl adj_lvl(const JmgPlan* p, void* aws, const AdjLayout& L, int l) {
+  double* b = ptr<double>(aws, L.lvl[l]);
+  const size_t n = p->lv[l].elems;
+  return AdjLvl{b, b + n, b + 2 * n, b + 3 * n, b + 4 * n, b + 5 * n};
+}
+
+int fail(int code, const char* m) { return set_error_message(code, m); }
+
+#define JMG_ACUDA(call)                                                   \
+  do {                                                                    \
+    cudaError_t e_ = (call);                                              \
+    if (e_ != cudaSuccess) return fail(JMG_ERR_CUDA, cudaGetErrorString(e_)); \
+  } while (0)
+
+// run the taped cycle forward on the workspace level arrays (phi_0 already loaded);
+// with snapshots, copy phi of the level after every sweep / prolongation
+void run_tape_forward(const JmgPlan* p, void* ws, void* aws, const AdjLayout& L, const Tape& t, bool snapshots,
+                      cudaStream_t s) {
+  const CycleParams cp = cycle_params(p, false);
+  // current buffer of every level (one-pass sweeps swap a level's two buffers)
+  std::vector<Lvl<double>> cur(p->used);
+  for (int l = 0; l < p->used; ++l) cur[l] = lvl64(p, ws, l);
+  for (const TapeOp& op : t.ops) {
+    Lvl<double>& a = cur[op.lev];
+    if (op.kind == OP_SWEEP) launch_sweep<double>(p->dim, a, s);
+    else if (op.kind == OP_RESTRICT) launch_restrict<double>(p->dim, a, cur[op.lev + 1], s);
+    else launch_prolong<double>(p->dim, a, cur[op.lev + 1], cp.diag, s);
+    if (snapshots && op.kind != OP_RESTRICT)
+      cudaMemcpyAsync(ptr<double>(aws, L.snap[op.after]), a.phi, p->lv[op.lev].elems * 8, cudaMemcpyDeviceToDevice, s);
+  }
+  const Lvl<double> first = lvl64(p, ws, 0);
+  if (cur[0].phi != first.phi)
+    cudaMemcpyAsync(first.phi, cur[0].phi, p->lv[0].elems * 8, cudaMemcpyDeviceToDevice, s);
+}
+
+}  // namespace
+}  // namespace jmg
+
+using namespace jmg;
+
+extern "C" {
+
+size_t jmg_adjoint_workspace_bytes(const JmgPlan* p) {
+  if (!p) return 0;
+  return adj_layout(p, make_tape(p)).total;
+}
+
+int jmg_solve_fixed_vjp(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs* c, const double* phi_bar,
+                        double* phi0_bar, double* rhs_bar, double* lam_bar, double* Dxx_bar, double* Dyy_bar,
+                        void* ws, size_t ws_bytes, void* aws, size_t aws_bytes, jmg_stream_t stream) {
+  int rc = check_ws(p, ws, ws_bytes);
+  if (rc) return rc;
+  if (p->dim != 2) return fail(JMG_ERR_VALUE, "the adjoint is implemented for 2D solves");
+  if (!p->cfg.fixed) return fail(JMG_ERR_VALUE, "reverse mode needs fixed mode (as in the reference)");
+  if (p->mixed) return fail(JMG_ERR_VALUE, "the adjoint differentiates the FP64 method (precision fp64)");
+  if ((rc = check_coeffs(p, c))) return rc;
+  if (!c->lam || !c->D[0] || !c->D[1])
+    return fail(JMG_ERR_VALUE, "the adjoint needs lambda, D_xx and D_yy as arrays (broadcast scalars first)");
+  if (!phi0 || !rhs || !phi_bar || !phi0_bar || !rhs_bar || !lam_bar || !Dxx_bar || !Dyy_bar)
+    return fail(JMG_ERR_VALUE, "NULL array argument");
+  const Tape tape = make_tape(p);
+  const AdjLayout L = adj_layout(p, tape);
+  if (!aws || aws_bytes < L.total || reinterpret_cast<uintptr_t>(aws) % kAlign)
+    return fail(JMG_ERR_WORKSPACE, "adjoint workspace missing, too small or misaligned");
+  cudaStream_t s = (cudaStream_t)stream;
+  const Box b0 = p->lv[0].box;
+  const size_t e0 = p->lv[0].elems;
+  const size_t dense = (size_t)b0.nx * b0.ny * b0.nz;
+  Lvl<double> l0 = lvl64(p, ws, 0);
+  const CycleParams cp = cycle_params(p, false);
+  const int nu1 = p->cfg.nu1 > 0 ? p->cfg.nu1 : 0;
+
+  // forward with checkpoints
+  launch_copy_in(b0, phi0, l0.phi, 1, s);
+  launch_copy_in(b0, rhs, l0.rhs, 1, s);
+  if ((rc = build_hierarchy(p, c, ws, s))) return rc;
+  JMG_ACUDA(cudaMemsetAsync(aws, 0, L.total, s));
+  double* pre = ptr<double>(aws, L.pre);
+  if (p->cfg.skip_pre) {  // the one-off pre-smoothing (solver_2d.py:457-459)
+    JMG_ACUDA(cudaMemcpyAsync(pre, l0.phi, e0 * 8, cudaMemcpyDeviceToDevice, s));
+    Lvl<double> cur = l0;
+    for (int k = 0; k < nu1; ++k) {
+      launch_sweep<double>(2, cur, s);
+      JMG_ACUDA(cudaMemcpyAsync(pre + (size_t)(k + 1) * e0, cur.phi, e0 * 8, cudaMemcpyDeviceToDevice, s));
+    }
+    if (cur.phi != l0.phi) JMG_ACUDA(cudaMemcpyAsync(l0.phi, cur.phi, e0 * 8, cudaMemcpyDeviceToDevice, s));
+  }
+  double* ck = ptr<double>(aws, L.ckpt);
+  for (int k = 0; k < L.ncyc; ++k) {
+    // the loop body starts with do_BCs (solver_2d.py:462); the level-0 frame is already zero
+    JMG_ACUDA(cudaMemcpyAsync(ck + (size_t)k * e0, l0.phi, e0 * 8, cudaMemcpyDeviceToDevice, s));
+    run_tape_forward(p, ws, aws, L, tape, false, s);
+  }
+
+  // backward
+  std::vector<AdjLvl> g(p->used);
+  for (int l = 0; l < p->used; ++l) g[l] = adj_lvl(p, aws, L, l);
+  launch_copy_in(b0, phi_bar, g[0].pb, 1, s);  // the output's frame is a constant (do_BCs)
+  const double* zeros = ptr<double>(aws, L.zeros);
+  for (int k = L.ncyc - 1; k >= 0; --k) {
+    JMG_ACUDA(cudaMemcpyAsync(l0.phi, ck + (size_t)k * e0, e0 * 8, cudaMemcpyDeviceToDevice, s));
+    run_tape_forward(p, ws, aws, L, tape, true, s);
+    auto state = [&](int idx, int lev) -> const double* {
+      if (idx == kZeros) return zeros;
+      if (idx == kInput) return ck + (size_t)k * e0;
+      (void)lev;
+      return ptr<double>(aws, L.snap[idx]);
+    };
+    for (int t = (int)tape.ops.size() - 1; t >= 0; --t) {
+      const TapeOp& op = tape.ops[t];
+      Lvl<double> a = lvl64(p, ws, op.lev);
+      if (op.kind == OP_SWEEP) {
+        adj_sweep(a, g[op.lev], state(op.before, op.lev), state(op.after, op.lev), s);
+      } else if (op.kind == OP_PROLONG) {
+        adj_prolong(a, g[op.lev], lvl64(p, ws, op.lev + 1), g[op.lev + 1], cp.diag, s);
+      } else {
+        adj_restrict(a, g[op.lev], state(op.before, op.lev), lvl64(p, ws, op.lev + 1), g[op.lev + 1], s);
+      }
+    }
+  }
+  if (p->cfg.skip_pre)
+    for (int k = nu1 - 1; k >= 0; --k) adj_sweep(l0, g[0], pre + (size_t)k * e0, pre + (size_t)(k + 1) * e0, s);
+
+  // adjoints of the inputs: phi0, rhs (level 0), then the coefficient hierarchy
+  launch_copy_out(b0, g[0].pb, phi0_bar, s);
+  launch_copy_out(b0, g[0].rb, rhs_bar, s);
+  JMG_ACUDA(cudaMemsetAsync(lam_bar, 0, dense * 8, s));
+  JMG_ACUDA(cudaMemsetAsync(Dxx_bar, 0, dense * 8, s));
+  JMG_ACUDA(cudaMemsetAsync(Dyy_bar, 0, dense * 8, s));
+  for (int l = 0; l < p->used; ++l) {
+    const double ix = p->grid.idel[0] * std::pow(0.5, l), iy = p->grid.idel[1] * std::pow(0.5, l);
+    adj_hierarchy2d(lvl64(p, ws, l), g[l], l, ix * ix, iy * iy, b0.nx, Dxx_bar, Dyy_bar, lam_bar, s);
+  }
+  JMG_ACUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
+}  // extern "C"

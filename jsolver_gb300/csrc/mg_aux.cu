@@ -142,9 +142,10 @@ __device__ __forceinline__ double block_sum(double v) {
   return v;
 }
 
-// sum over interior points of d^2, d = rhs - L_h phi (phi == nullptr: d = rhs)
+// sum over interior points of d^2, d = rhs - L_h phi (phi == nullptr: d = rhs); with r32,
+// d is also stored as FP32 (the right-hand side of the next refinement step)
 template <typename T, int DIM>
-__global__ void k_residual_partials(Lvl<T> a, const T* phi, double* parts) {
+__global__ void k_residual_partials(Lvl<T> a, const T* phi, double* parts, float* r32) {
   const int nx = a.mx - 1, ny = a.my - 1, nz = DIM == 3 ? a.mz - 1 : 1;
   const long long n = (long long)nx * ny * nz;
   double acc = 0.0;
@@ -157,6 +158,7 @@ __global__ void k_residual_partials(Lvl<T> a, const T* phi, double* parts) {
     if (phi == nullptr) d = (double)a.rhs[p];
     else if (DIM == 2) d = (double)defect_point2d<T>(phi, a.rhs, a.wx, a.wy, a.acc, p, a.P);
     else d = (double)defect_point3d<T>(phi, a.rhs, a.wx, a.wy, a.wz, a.acc, p, a.P, a.S);
+    if (r32) r32[p] = (float)d;
     acc = fma(d, d, acc);
   }
   acc = block_sum(acc);
@@ -164,13 +166,15 @@ __global__ void k_residual_partials(Lvl<T> a, const T* phi, double* parts) {
 }
 
 template <typename T>
-void launch_residual_partials(int dim, const Lvl<T>& a, const T* phi_or_null, double* parts, int, cudaStream_t s) {
+void launch_residual_partials(int dim, const Lvl<T>& a, const T* phi_or_null, double* parts, int, cudaStream_t s,
+                              float* r32) {
   if (dim == 2)
-    k_residual_partials<T, 2><<<kResBlocks, kResThreads, 0, s>>>(a, phi_or_null, parts);
+    k_residual_partials<T, 2><<<kResBlocks, kResThreads, 0, s>>>(a, phi_or_null, parts, r32);
   else
-    k_residual_partials<T, 3><<<kResBlocks, kResThreads, 0, s>>>(a, phi_or_null, parts);
+    k_residual_partials<T, 3><<<kResBlocks, kResThreads, 0, s>>>(a, phi_or_null, parts, r32);
 }
-template void launch_residual_partials<double>(int, const Lvl<double>&, const double*, double*, int, cudaStream_t);
+template void launch_residual_partials<double>(int, const Lvl<double>&, const double*, double*, int, cudaStream_t,
+                                               float*);
 
 __device__ double reduce_parts_warp(const double* parts, int n) {
   // called by one full warp; fixed assignment of parts to lanes, fixed shuffle tree

@@ -16,6 +16,7 @@
 
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -23,6 +24,7 @@
 
 #include "../../include/jmg.h"
 #include "mg_kernels.h"
+#include "mg_plan.h"
 
 using namespace jmg;
 
@@ -45,40 +47,6 @@ int set_err(int code, const char* fmt, ...) {
     cudaError_t e_ = (call);                                                                    \
     if (e_ != cudaSuccess) return set_err(JMG_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
   } while (0)
-
-constexpr size_t kAlign = 256;
-inline size_t align_up(size_t x, size_t a = kAlign) { return (x + a - 1) / a * a; }
-
-struct LevelInfo {
-  int m[3];
-  Box box;
-  size_t elems;
-  size_t phi, rhs, wx, wy, wz, invd, acc;   // FP64 arrays (byte offsets)
-  size_t d[3];                              // 3D averaged D (levels >= 1)
-  size_t phi32, rhs32, wx32, wy32, wz32, invd32, acc32;  // FP32 mirrors (mixed precision)
-};
-
-}  // namespace
-
-struct JmgPlan {
-  JmgGrid grid;
-  JmgConfig cfg;
-  int dim = 2;
-  int levels = 0;       // L of the reference
-  int used = 0;         // levels visited: 0..L-2
-  int coarse_start = 0; // first level run by the single-block kernel
-  bool mixed = false;
-  std::vector<LevelInfo> lv;
-  size_t off_phi_old = 0, off_state = 0, off_parts = 0, off_tab64 = 0, off_tab32 = 0, ws_bytes = 0;
-  int nparts = 0;
-  // graph cache
-  cudaGraphExec_t exec = nullptr;
-  void* exec_ws = nullptr;
-  int exec_mode = -1;
-  cudaStream_t cap = nullptr;
-};
-
-namespace {
 
 int validate_and_layout(JmgPlan* p) {
   const JmgGrid& g = p->grid;
@@ -154,7 +122,11 @@ int validate_and_layout(JmgPlan* p) {
   p->off_phi_old = take(p->lv[0].elems * 8);
   p->off_state = take(sizeof(LoopState));
   p->nparts = residual_num_parts(d, p->lv[0].box);
-  p->off_parts = take((size_t)p->nparts * 8 + 64);
+  {
+    const int fused_parts = d == 2 ? residual_f32_parts2d(p->lv[0].m[0], p->lv[0].m[1]) : 0;
+    const int maxparts = p->nparts > fused_parts ? p->nparts : fused_parts;
+    p->off_parts = take((size_t)maxparts * 8 + 64);
+  }
   p->off_tab64 = take(sizeof(LvlTable<double>));
   p->off_tab32 = take(sizeof(LvlTable<float>));
   p->ws_bytes = off;
@@ -168,15 +140,21 @@ int validate_and_layout(JmgPlan* p) {
     }
   }
   p->coarse_start = cs;
+  {
+    const int m0[3] = {g.m[0], g.m[1], d == 3 ? g.m[2] : 0};
+    const size_t limit = 200 * 1024;
+    const size_t b64 = coarse_smem_bytes(d, m0, cs, L - 2, 8), b32 = coarse_smem_bytes(d, m0, cs, L - 2, 4);
+    p->coarse_smem64 = b64 <= limit ? b64 : 0;
+    p->coarse_smem32 = b32 <= limit ? b32 : 0;
+  }
+  const char* hl = getenv("JMG_HOST_LOOP");
+  p->host_loop = hl && hl[0] == '1';
   return JMG_OK;
 }
 
-template <typename T>
-T* ptr(void* ws, size_t off) {
-  return reinterpret_cast<T*>(static_cast<char*>(ws) + off);
-}
 
-Lvl<double> lvl64(const JmgPlan* p, void* ws, int l) {
+}  // namespace
+Lvl<double> jmg::lvl64(const JmgPlan* p, void* ws, int l) {
   const LevelInfo& li = p->lv[l];
   Lvl<double> a;
   a.phi = ptr<double>(ws, li.phi);
@@ -193,8 +171,10 @@ Lvl<double> lvl64(const JmgPlan* p, void* ws, int l) {
   a.S = li.box.S;
   return a;
 }
+namespace {
 
-Lvl<float> lvl32(const JmgPlan* p, void* ws, int l) {
+}  // namespace
+Lvl<float> jmg::lvl32(const JmgPlan* p, void* ws, int l) {
   const LevelInfo& li = p->lv[l];
   Lvl<float> a;
   a.phi = ptr<float>(ws, li.phi32);
@@ -211,6 +191,7 @@ Lvl<float> lvl32(const JmgPlan* p, void* ws, int l) {
   a.S = li.box.S;
   return a;
 }
+namespace {
 
 template <typename T>
 LvlTable<T> make_table(const JmgPlan* p, void* ws);
@@ -229,7 +210,8 @@ LvlTable<float> make_table<float>(const JmgPlan* p, void* ws) {
   return t;
 }
 
-CycleParams cycle_params(const JmgPlan* p, bool off_diag) {
+}  // namespace
+CycleParams jmg::cycle_params(const JmgPlan* p, bool off_diag) {
   CycleParams cp;
   cp.last_level = p->levels - 2;
   cp.nu1 = p->cfg.nu1 > 0 ? p->cfg.nu1 : 0;
@@ -240,28 +222,40 @@ CycleParams cycle_params(const JmgPlan* p, bool off_diag) {
   cp.diag = (p->cfg.nu2 <= 0 || off_diag) ? 1 : 0;
   return cp;
 }
+namespace {
+
+// multigrid_cycle, solver_2d.py:582-614, emitted as launches on stream s. With a
+// non-null `count`, nothing is launched and the number of kernel launches is added.
+// Option of the outermost call of a cycle (level 0 only): start the first sweep from a
+// zero guess without reading phi (a refinement step's correction).
+struct EmitTop {
+  bool zero_first = false;
+};
 
 // multigrid_cycle, solver_2d.py:582-614, emitted as launches on stream s. With a
 // non-null `count`, nothing is launched and the number of kernel launches is added.
 template <typename T>
-void emit_cycle(const JmgPlan* p, const LvlTable<T>& tab, const LvlTable<T>* dtab, const CycleParams& cp, int lev,
-                bool fcycle, bool skip_pre, cudaStream_t s, long long* count = nullptr) {
+void emit_cycle(const JmgPlan* p, LvlTable<T>& tab, const LvlTable<T>* dtab, const CycleParams& cp, int lev,
+                bool fcycle, bool skip_pre, cudaStream_t s, long long* count = nullptr,
+                const EmitTop* top = nullptr) {
   const int dim = p->dim;
-  auto sweep = [&]() {
-    if (count) *count += 2;
-    else launch_sweep<T>(dim, tab.l[lev], s);
+  auto sweep = [&](bool first) {
+    if (count) *count += 2;  // two colour passes
+    else launch_sweep<T>(dim, tab.l[lev], s, top && top->zero_first && first);
   };
   if (lev >= p->coarse_start) {
+    const size_t smem = sizeof(T) == 8 ? p->coarse_smem64 : p->coarse_smem32;
     if (count) *count += 1;
+    else if (smem) launch_coarse_smem<T>(dim, dtab, cp, lev, fcycle ? 1 : 0, skip_pre ? 1 : 0, smem, s);
     else launch_coarse_cycle<T>(dim, dtab, cp, lev, fcycle ? 1 : 0, skip_pre ? 1 : 0, s);
     return;
   }
   if (lev == cp.last_level) {
-    for (int k = 0; k < cp.nu1 + cp.nu2; ++k) sweep();
+    for (int k = 0; k < cp.nu1 + cp.nu2; ++k) sweep(k == 0);
     return;
   }
   if (!skip_pre)
-    for (int k = 0; k < cp.nu1; ++k) sweep();
+    for (int k = 0; k < cp.nu1; ++k) sweep(k == 0);
   if (count) *count += 1;
   else launch_restrict<T>(dim, tab.l[lev], tab.l[lev + 1], s);
   if (fcycle)
@@ -269,7 +263,21 @@ void emit_cycle(const JmgPlan* p, const LvlTable<T>& tab, const LvlTable<T>* dta
   for (int g = 0; g < cp.gamma; ++g) emit_cycle<T>(p, tab, dtab, cp, lev + 1, false, false, s, count);
   if (count) *count += 1;
   else launch_prolong<T>(dim, tab.l[lev], tab.l[lev + 1], cp.diag, s);
-  for (int k = 0; k < cp.nu2; ++k) sweep();
+  for (int k = 0; k < cp.nu2; ++k) sweep(false);
+}
+
+// Whether the mixed-precision refinement step can use the short form: the FP32 cycle
+// starts with a sweep at level 0 from a zero guess (no zeroing pass), and one tiled FP64
+// kernel gives both the stopping test's residual and the next step's FP32 right-hand side.
+bool mixed_fused(const JmgPlan* p) {
+  return p->mixed && p->dim == 2 && p->cfg.stop == JMG_STOP_RESIDUAL && !p->cfg.fixed && p->coarse_start > 0 &&
+         p->cfg.nu1 >= 1 && p->cfg.nu2 >= 1;
+}
+
+// Mixed precision with the residual stop in any other case (3D, small grids, nu = 0):
+// one FP64 pass computes the residual norm and the FP32 right-hand side together.
+bool mixed_resid(const JmgPlan* p) {
+  return p->mixed && !mixed_fused(p) && p->cfg.stop == JMG_STOP_RESIDUAL && !p->cfg.fixed;
 }
 
 int loop_mode(const JmgPlan* p) {
@@ -284,24 +292,61 @@ void emit_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaStream
   double* parts = ptr<double>(ws, p->off_parts);
   Lvl<double> l0 = lvl64(p, ws, 0);
   CycleParams cp = cycle_params(p, false);
+  int nparts = p->nparts;
   if (!p->mixed) {
     LvlTable<double> tab = make_table<double>(p, ws);
     emit_cycle<double>(p, tab, ptr<LvlTable<double>>(ws, p->off_tab64), cp, 0, p->cfg.fcycle != 0,
                        p->cfg.skip_pre != 0, s);
+  } else if (mixed_fused(p)) {
+    // FP64 iterative refinement around FP32 cycles. r32 = float(rhs - L_h phi) is already
+    // in place (prologue or previous step). FP32 cycles solve L_h e = r from e = 0; the
+    // last sweep adds e to phi (FP64); then the FP64 residual for the next step and the
+    // stopping test.
+    LvlTable<float> t32 = make_table<float>(p, ws);
+    const int inner = p->cfg.inner_cycles > 0 ? p->cfg.inner_cycles : 1;
+    for (int k = 0; k < inner; ++k) {
+      EmitTop top;
+      top.zero_first = k == 0;
+      emit_cycle<float>(p, t32, ptr<LvlTable<float>>(ws, p->off_tab32), cp, 0, p->cfg.fcycle != 0, false, s,
+                        nullptr, &top);
+    }
+    launch_add_correction(p->dim, l0, t32.l[0].phi, s);
+    launch_residual_f32_2d(l0, t32.l[0].rhs, parts, s);
+    nparts = residual_f32_parts2d(l0.mx, l0.my);
   } else {
     // FP64 iterative refinement around FP32 cycles: r = rhs - L_h phi (FP64), solve
-    // L_h e = r with FP32 cycles from e = 0, phi += e (FP64)
+    // L_h e = r with FP32 cycles from e = 0, phi += e (FP64). With the residual stop, r32
+    // comes from the previous step's residual pass (or the prologue).
     LvlTable<float> t32 = make_table<float>(p, ws);
-    launch_residual_to_f32(p->dim, l0, t32.l[0].rhs, s);
+    if (!mixed_resid(p)) launch_residual_to_f32(p->dim, l0, t32.l[0].rhs, s);
     launch_zero_f32(p->lv[0].box, t32.l[0].phi, s);
     const int inner = p->cfg.inner_cycles > 0 ? p->cfg.inner_cycles : 1;
     for (int k = 0; k < inner; ++k)
       emit_cycle<float>(p, t32, ptr<LvlTable<float>>(ws, p->off_tab32), cp, 0, p->cfg.fcycle != 0, false, s);
     launch_add_correction(p->dim, l0, t32.l[0].phi, s);
+    if (mixed_resid(p)) launch_residual_partials<double>(p->dim, l0, l0.phi, parts, p->nparts, s, t32.l[0].rhs);
   }
   if (mode == 0) launch_distance_snapshot(p->lv[0].box, ptr<double>(ws, p->off_phi_old), l0.phi, st, s);
-  if (mode == 1) launch_residual_partials<double>(p->dim, l0, l0.phi, parts, p->nparts, s);
-  launch_loop_step(st, parts, p->nparts, mode, p->cfg.epsilon, p->cfg.rtol, p->cfg.max_iters_outer, handle, s);
+  if (mode == 1 && !p->mixed) launch_residual_partials<double>(p->dim, l0, l0.phi, parts, p->nparts, s);
+  launch_loop_step(st, parts, nparts, mode, p->cfg.epsilon, p->cfg.rtol, p->cfg.max_iters_outer, handle, s);
+}
+
+// loop prologue: initial residual (residual stop) and loop init
+void emit_prologue(const JmgPlan* p, void* ws, unsigned long long handle, cudaStream_t s) {
+  const int mode = loop_mode(p);
+  LoopState* st = ptr<LoopState>(ws, p->off_state);
+  double* parts = ptr<double>(ws, p->off_parts);
+  Lvl<double> l0 = lvl64(p, ws, 0);
+  int nparts = p->nparts;
+  if (mixed_fused(p)) {
+    launch_residual_f32_2d(l0, lvl32(p, ws, 0).rhs, parts, s);
+    nparts = residual_f32_parts2d(l0.mx, l0.my);
+  } else if (mixed_resid(p)) {
+    launch_residual_partials<double>(p->dim, l0, l0.phi, parts, p->nparts, s, lvl32(p, ws, 0).rhs);
+  } else if (mode == 1) {
+    launch_residual_partials<double>(p->dim, l0, l0.phi, parts, p->nparts, s);
+  }
+  launch_loop_init(st, parts, nparts, mode, p->cfg.rtol, p->cfg.max_iters_outer, handle, s);
 }
 
 long long body_launches(const JmgPlan* p) {
@@ -316,11 +361,11 @@ long long body_launches(const JmgPlan* p) {
     memset(&t, 0, sizeof(t));
     const int inner = p->cfg.inner_cycles > 0 ? p->cfg.inner_cycles : 1;
     for (int k = 0; k < inner; ++k) emit_cycle<float>(p, t, nullptr, cp, 0, p->cfg.fcycle != 0, false, nullptr, &n);
-    n += 3;  // residual_to_f32, zero, add_correction
+    n += mixed_fused(p) ? 2 : (mixed_resid(p) ? 3 : 3 + (loop_mode(p) == 0));
   }
   const int mode = loop_mode(p);
-  if (mode == 0 || mode == 1) n += 1;  // distance or residual partials
-  n += 1;                              // loop step
+  if (!p->mixed && (mode == 0 || mode == 1)) n += 1;  // distance or residual partials
+  n += 1;                                             // loop step
   return n;
 }
 
@@ -342,8 +387,7 @@ int build_graph(JmgPlan* p, void* ws) {
   JMG_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 0, 0));
   // prologue: initial residual (residual stop) and loop init, then the WHILE node
   JMG_CUDA(cudaStreamBeginCaptureToGraph(p->cap, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  if (mode == 1) launch_residual_partials<double>(p->dim, l0, l0.phi, parts, p->nparts, p->cap);
-  launch_loop_init(st, parts, p->nparts, mode, p->cfg.rtol, p->cfg.max_iters_outer, handle, p->cap);
+  emit_prologue(p, ws, handle, p->cap);
   cudaStreamCaptureStatus cst;
   const cudaGraphNode_t* deps = nullptr;
   size_t ndeps = 0;
@@ -386,7 +430,8 @@ HierInputs hier_inputs(const JmgPlan* p, const JmgCoeffs* c) {
   return in;
 }
 
-int check_coeffs(const JmgPlan* p, const JmgCoeffs* c) {
+}  // namespace
+int jmg::check_coeffs(const JmgPlan* p, const JmgCoeffs* c) {
   if (!c) return set_err(JMG_ERR_VALUE, "coeffs must not be NULL");
   int nscalar = 0;
   for (int a = 0; a < p->dim; ++a)
@@ -398,8 +443,10 @@ int check_coeffs(const JmgPlan* p, const JmgCoeffs* c) {
     return set_err(JMG_ERR_VALUE, "D_xy (9-point stencil) is not supported by this build");
   return JMG_OK;
 }
+namespace {
 
-int check_ws(const JmgPlan* p, void* ws, size_t bytes) {
+}  // namespace
+int jmg::check_ws(const JmgPlan* p, void* ws, size_t bytes) {
   if (!p) return set_err(JMG_ERR_VALUE, "plan must not be NULL");
   if (!ws || bytes < p->ws_bytes)
     return set_err(JMG_ERR_WORKSPACE, "workspace too small: %zu bytes given, %zu needed", bytes, p->ws_bytes);
@@ -407,9 +454,12 @@ int check_ws(const JmgPlan* p, void* ws, size_t bytes) {
     return set_err(JMG_ERR_WORKSPACE, "workspace must be %zu-byte aligned", kAlign);
   return JMG_OK;
 }
+namespace {
 
-int build_hierarchy(JmgPlan* p, const JmgCoeffs* c, void* ws, cudaStream_t s) {
+}  // namespace
+int jmg::build_hierarchy(JmgPlan* p, const JmgCoeffs* c, void* ws, cudaStream_t s) {
   const HierInputs in = hier_inputs(p, c);
+
   const Box b0 = p->lv[0].box;
   for (int l = 0; l < p->used; ++l) {
     const LevelInfo& li = p->lv[l];
@@ -445,6 +495,7 @@ int build_hierarchy(JmgPlan* p, const JmgCoeffs* c, void* ws, cudaStream_t s) {
   JMG_CUDA(cudaGetLastError());
   return JMG_OK;
 }
+namespace {
 
 __global__ void k_write_i64(long long* out, long long v) { *out = v; }
 
@@ -529,7 +580,12 @@ int jmg_solve(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs
   // 2. coefficients, and the level tables the single-block coarse kernel reads
   if ((rc = build_hierarchy(p, c, ws, s))) return rc;
   launch_store_table<double>(make_table<double>(p, ws), ptr<LvlTable<double>>(ws, p->off_tab64), s);
-  if (p->mixed) launch_store_table<float>(make_table<float>(p, ws), ptr<LvlTable<float>>(ws, p->off_tab32), s);
+  if (p->mixed) {
+    launch_store_table<float>(make_table<float>(p, ws), ptr<LvlTable<float>>(ws, p->off_tab32), s);
+    // zero frames of the FP32 correction and residual of level 0 (kernels write only interiors)
+    launch_zero_f32(b0, lvl32(p, ws, 0).phi, s);
+    launch_zero_f32(b0, lvl32(p, ws, 0).rhs, s);
+  }
   if (mode == 1) {
     launch_residual_partials<double>(p->dim, l0, nullptr, parts, p->nparts, s);
     launch_rhs_norm(st, parts, p->nparts, s);
@@ -538,14 +594,28 @@ int jmg_solve(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs
   const int nu1 = p->cfg.nu1 > 0 ? p->cfg.nu1 : 0;
   const bool presmoothed = p->cfg.skip_pre && nu1 > 0;
   if (presmoothed) {
-    for (int k = 0; k < nu1; ++k) launch_sweep<double>(p->dim, l0, s);
+    Lvl<double> cur = l0;
+    for (int k = 0; k < nu1; ++k) launch_sweep<double>(p->dim, cur, s);
     launch_distance_snapshot(b0, phi_old, l0.phi, st, s);  // phi_old <- smoothed phi
   }
   // 4. the loop
+  if (p->coarse_smem64 && prepare_coarse_smem<double>(p->dim, p->coarse_smem64))
+    return set_err(JMG_ERR_CUDA, "cannot enable %zu bytes of shared memory for the coarse kernel", p->coarse_smem64);
+  if (p->mixed && p->coarse_smem32 && prepare_coarse_smem<float>(p->dim, p->coarse_smem32))
+    return set_err(JMG_ERR_CUDA, "cannot enable %zu bytes of shared memory for the coarse kernel", p->coarse_smem32);
   const bool runs = p->cfg.max_iters_outer > 0;
-  if (runs) {
+  if (runs && !p->host_loop) {
     if ((rc = build_graph(p, ws))) return rc;
     JMG_CUDA(cudaGraphLaunch(p->exec, s));
+  } else if (runs) {
+    emit_prologue(p, ws, 0, s);
+    for (;;) {
+      int go = 0;
+      JMG_CUDA(cudaMemcpyAsync(&go, &st->go, sizeof(int), cudaMemcpyDeviceToHost, s));
+      JMG_CUDA(cudaStreamSynchronize(s));
+      if (!go) break;
+      emit_body(p, ws, 0, s);
+    }
   }
   // 5. outputs. With no cycle and no smoothing the reference returns phi0 untouched.
   if (runs || presmoothed)
@@ -696,7 +766,7 @@ int jmg_plan_launch_counts(const JmgPlan* p, int64_t* per_solve_fixed, int64_t* 
   if (!p) return set_err(JMG_ERR_VALUE, "plan must not be NULL");
   // copy-ins (3), hierarchy (2 per level + FP32 conversions), rhs norm (2), loop init
   // (1-2), copy-out and count (2)
-  long long fixed = 3 + 2LL * p->used + 2 + 2 + (p->mixed ? 2 : 1);
+  long long fixed = 3 + 2LL * p->used + 2 + 2 + (p->mixed ? 4 : 1);
   if (p->mixed) fixed += (long long)p->used * (p->dim == 3 ? 5 : 4);
   if (loop_mode(p) == 1) fixed += 2 + 1;
   fixed += 1;

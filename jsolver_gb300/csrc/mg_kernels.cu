@@ -18,20 +18,23 @@ namespace jmg {
 // grid-wide operators
 // ------------------------------------------------------------------------------------
 
-// 2D: blockDim (64, 4); x walks the points of one colour in a row, y walks rows.
+// 2D: blockDim (64, 4); x walks the points of one colour in a row, y walks rows. With
+// zero_other, the other colour is taken as zero without being read: the first colour
+// pass of a sweep from a zero initial guess (a refinement step's correction).
 template <typename T>
-__global__ void k_sweep_color2d(Lvl<T> a, int color) {
+__global__ void k_sweep_color2d(Lvl<T> a, int color, int zero_other) {
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
   if (i > a.my) return;
   const int j = 2 + ((i + color) & 1) + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
   if (j > a.mx) return;
   const long long p = (long long)i * a.P + j;
-  a.phi[p] = gs_point2d<T>(a.phi, a.rhs, a.wx, a.wy, a.invd, p, a.P);
+  // with all neighbours zero, (0 - rhs) / A_cc is what the full expression gives
+  a.phi[p] = zero_other ? (T(0) - a.rhs[p]) * a.invd[p] : gs_point2d<T>(a.phi, a.rhs, a.wx, a.wy, a.invd, p, a.P);
 }
 
 // 3D: blockDim (64, 4, 1); grid z walks planes.
 template <typename T>
-__global__ void k_sweep_color3d(Lvl<T> a, int color) {
+__global__ void k_sweep_color3d(Lvl<T> a, int color, int zero_other) {
   const int k = blockIdx.z + 2;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
   if (j > a.my || k > a.mz) return;
@@ -40,7 +43,8 @@ __global__ void k_sweep_color3d(Lvl<T> a, int color) {
   const int i = 2 + ((j + k + par) & 1) + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
   if (i > a.mx) return;
   const long long p = (long long)k * a.S + (long long)j * a.P + i;
-  a.phi[p] = gs_point3d<T>(a.phi, a.rhs, a.wx, a.wy, a.wz, a.invd, p, a.P, a.S);
+  a.phi[p] = zero_other ? (T(0) - a.rhs[p]) * a.invd[p]
+                        : gs_point3d<T>(a.phi, a.rhs, a.wx, a.wy, a.wz, a.invd, p, a.P, a.S);
 }
 
 // Over the full padded coarse array: phi_c = 0, rhs_c = restricted defect inside, 0 on the frame.
@@ -238,15 +242,19 @@ __global__ void k_store_table(LvlTable<T> tab, LvlTable<T>* dst) {
 
 static inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
+// One full sweep: the red colour pass, then the black one, in place (a colour pass reads
+// only the other colour, so it needs no second buffer). With zero_init the sweep starts
+// from phi = 0 (the red pass does not read phi). a.phi holds the result on return.
 template <typename T>
-void launch_sweep(int dim, const Lvl<T>& a, cudaStream_t s) {
+void launch_sweep(int dim, Lvl<T>& a, cudaStream_t s, bool zero_init) {
   for (int color = 0; color < 2; ++color) {
+    const int zero = (zero_init && color == 0) ? 1 : 0;
     if (dim == 2) {
       dim3 b(64, 4), g(cdiv(a.mx / 2, 64), cdiv(a.my - 1, 4));
-      k_sweep_color2d<T><<<g, b, 0, s>>>(a, color);
+      k_sweep_color2d<T><<<g, b, 0, s>>>(a, color, zero);
     } else {
       dim3 b(64, 4, 1), g(cdiv(a.mx / 2, 64), cdiv(a.my - 1, 4), a.mz - 1);
-      k_sweep_color3d<T><<<g, b, 0, s>>>(a, color);
+      k_sweep_color3d<T><<<g, b, 0, s>>>(a, color, zero);
     }
   }
 }
@@ -254,8 +262,7 @@ void launch_sweep(int dim, const Lvl<T>& a, cudaStream_t s) {
 template <typename T>
 void launch_restrict(int dim, const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s) {
   if (dim == 2) {
-    dim3 b(32, 8), g(cdiv(c.mx + 3, 32), cdiv(c.my + 3, 8));
-    k_restrict2d<T><<<g, b, 0, s>>>(f, c);
+    launch_restrict_tile2d<T>(f, c, s);
   } else {
     dim3 b(32, 8, 1), g(cdiv(c.mx + 3, 32), cdiv(c.my + 3, 8), c.mz + 3);
     k_restrict3d<T><<<g, b, 0, s>>>(f, c);
@@ -288,7 +295,7 @@ void launch_store_table(const LvlTable<T>& tab, LvlTable<T>* dst, cudaStream_t s
 }
 
 #define JMG_INST(T)                                                                               \
-  template void launch_sweep<T>(int, const Lvl<T>&, cudaStream_t);                                \
+  template void launch_sweep<T>(int, Lvl<T>&, cudaStream_t, bool);                                \
   template void launch_restrict<T>(int, const Lvl<T>&, const Lvl<T>&, cudaStream_t);              \
   template void launch_prolong<T>(int, const Lvl<T>&, const Lvl<T>&, int, cudaStream_t);          \
   template void launch_coarse_cycle<T>(int, const LvlTable<T>*, const CycleParams&, int, int, int, cudaStream_t); \

@@ -24,12 +24,25 @@ struct LoopState {
   int pad;
 };
 
-template <typename T> void launch_sweep(int dim, const Lvl<T>& a, cudaStream_t s);
+// one full sweep (two colour passes, in place); with zero_init it starts from phi = 0
+template <typename T> void launch_sweep(int dim, Lvl<T>& a, cudaStream_t s, bool zero_init = false);
+// mg_tile2d.cu: defect + restriction with every fine defect computed once
+template <typename T> void launch_restrict_tile2d(const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s);
+// mg_tile2d.cu: r32 = float(rhs - L_h phi) (FP64 arithmetic) on the interior, and per-block
+// sums of r^2 into parts[0 .. residual_f32_parts2d(mx, my))
+int residual_f32_parts2d(int mx, int my);
+void launch_residual_f32_2d(const Lvl<double>& a, float* r32, double* parts, cudaStream_t s);
 template <typename T> void launch_restrict(int dim, const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s);
 template <typename T> void launch_prolong(int dim, const Lvl<T>& f, const Lvl<T>& c, int diag, cudaStream_t s);
 template <typename T>
 void launch_coarse_cycle(int dim, const LvlTable<T>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
                          cudaStream_t s);
+// mg_coarse.cu: the coarse sub-cycle from shared memory (one block)
+size_t coarse_smem_bytes(int dim, const int* m0, int lev0, int last, size_t elem);
+template <typename T> int prepare_coarse_smem(int dim, size_t bytes);
+template <typename T>
+void launch_coarse_smem(int dim, const LvlTable<T>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
+                        size_t smem, cudaStream_t s);
 // copies a level table into device memory (the coarse kernel reads it from there)
 template <typename T> void launch_store_table(const LvlTable<T>& tab, LvlTable<T>* dst, cudaStream_t s);
 
@@ -47,7 +60,7 @@ void launch_distance_snapshot(const Box& b, double* old_phi, const double* phi, 
 // partial sums of squares of the defect (or of rhs when phi == nullptr) over the interior
 template <typename T>
 void launch_residual_partials(int dim, const Lvl<T>& a, const T* phi_or_null, double* partials, int nparts,
-                              cudaStream_t s);
+                              cudaStream_t s, float* r32 = nullptr);
 int residual_num_parts(int dim, const Box& b);
 // device-side loop decisions
 void launch_loop_init(LoopState* st, const double* partials, int nparts, int mode, double rtol,

@@ -1,0 +1,69 @@
+// mg_plan.h — the plan object behind the C ABI (internal to libjmg).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/jmg.h"
+#include "mg_kernels.h"
+
+namespace jmg {
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t x, size_t a = kAlign) { return (x + a - 1) / a * a; }
+
+struct LevelInfo {
+  int m[3];
+  Box box;
+  size_t elems;
+  size_t phi, rhs, wx, wy, wz, invd, acc;   // FP64 arrays (byte offsets)
+  size_t d[3];                              // 3D averaged D (levels >= 1)
+  size_t phi32, rhs32, wx32, wy32, wz32, invd32, acc32;  // FP32 mirrors (mixed precision)
+};
+
+}  // namespace jmg
+
+struct JmgPlan {
+  JmgGrid grid;
+  JmgConfig cfg;
+  int dim = 2;
+  int levels = 0;       // L of the reference
+  int used = 0;         // levels visited: 0..L-2
+  int coarse_start = 0; // first level run by the single-block kernel
+  bool mixed = false;
+  std::vector<jmg::LevelInfo> lv;
+  size_t off_phi_old = 0, off_state = 0, off_parts = 0, off_tab64 = 0, off_tab32 = 0, ws_bytes = 0;
+  int nparts = 0;
+  // graph cache
+  cudaGraphExec_t exec = nullptr;
+  void* exec_ws = nullptr;
+  int exec_mode = -1;
+  cudaStream_t cap = nullptr;
+  // Host-driven loop instead of the conditional-WHILE graph (environment variable
+  // JMG_HOST_LOOP=1 at plan creation): the same kernels, with the loop decision read back
+  // after every iteration. Profilers cannot attribute kernel nodes inside graphs that hold
+  // conditional nodes; this mode lets them see every launch.
+  bool host_loop = false;
+  // shared-memory bytes of the coarse sub-cycle kernel per precision (0: use the
+  // global-memory version, e.g. when the levels do not fit in shared memory)
+  size_t coarse_smem64 = 0, coarse_smem32 = 0;
+};
+
+
+namespace jmg {
+
+template <typename T>
+inline T* ptr(void* ws, size_t off) {
+  return reinterpret_cast<T*>(static_cast<char*>(ws) + off);
+}
+
+// views of level l of the workspace (mg_driver.cu)
+Lvl<double> lvl64(const JmgPlan* p, void* ws, int l);
+Lvl<float> lvl32(const JmgPlan* p, void* ws, int l);
+CycleParams cycle_params(const JmgPlan* p, bool off_diag);
+// validation of a solve's coefficient arguments and workspace (mg_driver.cu)
+int check_coeffs(const JmgPlan* p, const JmgCoeffs* c);
+int check_ws(const JmgPlan* p, void* ws, size_t bytes);
+int build_hierarchy(JmgPlan* p, const JmgCoeffs* c, void* ws, cudaStream_t s);
+
+}  // namespace jmg

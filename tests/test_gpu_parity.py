@@ -351,8 +351,10 @@ def test_mixed_precision_reaches_rtol():
     o = mg2d.Oracle2D(g, g)
     o.setup(*args)
     assert o.rel_residual(phim, p["rhs"]) <= 1e-10
-    # both are within the solver tolerance of the exact discrete solution
-    assert rel_l2(phim, phi64) < 1e-8
+    # both meet the residual tolerance; their difference is bounded by the operator's
+    # conditioning times 1e-10 and is far below the discretisation error
+    assert rel_l2(phim, phi64) < 1e-6
+    assert rel_l2(phim, p["phi_exact"]) < 1e-6
     assert cm <= c64 + 5
 
 
@@ -392,3 +394,36 @@ def test_do_bcs_device():
     np.testing.assert_array_equal(bc2(a).cpu().numpy(), mg2d.do_bcs(np.ones((131, 131))))
     b = torch.ones((11, 19, 7), dtype=torch.float64, device=DEV)
     np.testing.assert_array_equal(bc3(b).cpu().numpy(), mg3d.do_bcs(np.ones((11, 19, 7))))
+
+
+def test_mixed_precision_3d_reaches_rtol():
+    p = W.random_3d(32, seed=4)
+    g = grid_1D(32)
+    args = (p["phi0"], p["rhs"], p["lam"], p["D_xx"], p["D_yy"], p["D_zz"])
+    phi64, c64 = solve_3d(g, g, g, *args, stop="residual", rtol=1e-10, fcycle=True)
+    phim, cm = solve_3d(g, g, g, *args, stop="residual", rtol=1e-10, fcycle=True, precision="mixed")
+    o = mg3d.Oracle3D(g, g, g)
+    o.setup(*args)
+    assert o.rel_residual(phim, p["rhs"]) <= 1e-10
+    assert rel_l2(phim, phi64) < 1e-6
+    assert cm <= c64 + 5
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_mixed_precision_fixed_and_distance_modes(dim):
+    """The unfused refinement path (fixed count, distance stop) also converges to the FP64 answer."""
+    if dim == 2:
+        p = W.random_2d(64, seed=6)
+        gs = (grid_1D(64),) * 2
+        args = (p["phi0"], p["rhs"], p["lam"], p["D_xx"], p["D_yy"])
+        solve = solve_2d
+    else:
+        p = W.random_3d(16, seed=6)
+        gs = (grid_1D(16),) * 3
+        args = (p["phi0"], p["rhs"], p["lam"], p["D_xx"], p["D_yy"], p["D_zz"])
+        solve = solve_3d
+    ref, _ = solve(*gs, *args, stop="residual", rtol=1e-11)
+    phim, cm = solve(*gs, *args, precision="mixed", epsilon=1e-13)
+    assert rel_l2(phim, ref) < 1e-7
+    phif, cf = solve(*gs, *args, precision="mixed", fixed=True, max_iters_outer=cm)
+    assert cf == cm and rel_l2(phif, phim) < 1e-12
