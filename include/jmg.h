@@ -187,6 +187,46 @@ int jmg_plan_launch_counts(const JmgPlan* plan, int64_t* per_solve_fixed, int64_
 int jmg_rel_residual_noalloc(const JmgGrid* grid, const double* phi, const double* rhs,
                              const JmgCoeffs* coeffs, double* out, jmg_stream_t stream);
 
+/* ---- learned initial guess (2D) ---------------------------------------------------------
+ * No counterpart in the reference, which always starts from the caller's phi0: these
+ * entries predict phi0 with a small U-Net (4 levels, 16/32/64/64 channels, 3x3
+ * convolutions, BF16 activations and weights, FP32 accumulation on the tensor cores) and
+ * train it. The solver then iterates from that guess to the caller's tolerance, so the
+ * multigrid residual judges the guess. All pointers are device pointers; x is BF16 NHWC
+ * with 16 channels (16-byte aligned), y and targets are FP32 [batch][res][res]. */
+typedef struct JmgNet JmgNet;
+/* Number of FP32 parameters: per layer the weights [cout][3][3][cin], then the bias. */
+int64_t jmg_net_num_params(void);
+/* res: network resolution (a multiple of 128); max_batch: largest batch of the
+ * training and gradient calls. Parameters start at zero (set them before use). */
+int jmg_net_create(JmgNet** out, int res, int max_batch);
+void jmg_net_destroy(JmgNet* net);
+/* Copies parameters in (and resets the optimiser state) / out. */
+int jmg_net_set_params(JmgNet* net, const float* params, jmg_stream_t stream);
+int jmg_net_get_params(JmgNet* net, float* params, jmg_stream_t stream);
+/* y = network output (channel 0) for a batch of packed inputs. */
+int jmg_net_forward(JmgNet* net, const void* x, int batch, float* y, jmg_stream_t stream);
+/* Mean squared error against targets: *loss (device float) and, if grads is not NULL,
+ * d loss / d params (FP32, jmg_net_num_params values). */
+int jmg_net_loss_grad(JmgNet* net, const void* x, const float* target, int batch, float* loss, float* grads,
+                      jmg_stream_t stream);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) on the mean squared error; the batch's
+ * loss is added to *loss when loss is not NULL. */
+int jmg_net_train_step(JmgNet* net, const void* x, const float* target, int batch, float lr, float* loss,
+                       jmg_stream_t stream);
+/* Packed network input of one square 2D problem (grid m a multiple of res): averages
+ * over f x f blocks (f = m / res) of log D_xx, log D_yy, lambda / 10 and rhs, the last
+ * divided by its RMS over the network grid, written to *rms_out (device float). */
+int jmg_net_inputs_2d(JmgNet* net, const JmgGrid* grid, const JmgCoeffs* coeffs, const double* rhs, void* x,
+                      float* rms_out, jmg_stream_t stream);
+/* Training target of one problem: the block average of phi divided by out_scale * rms. */
+int jmg_net_target_2d(JmgNet* net, const JmgGrid* grid, const double* phi, const float* rms, float out_scale,
+                      float* target, jmg_stream_t stream);
+/* phi0 (dense padded (m+3)^2 FP64) = out_scale * rms * the network output, bilinear
+ * from the network grid to the solver grid, zero frame. */
+int jmg_net_guess_2d(JmgNet* net, const JmgGrid* grid, const JmgCoeffs* coeffs, const double* rhs, float out_scale,
+                     double* phi0, jmg_stream_t stream);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* jmg_last_error(void);
 

@@ -60,6 +60,18 @@ _SIGS = {
     "jmg_adjoint_workspace_bytes": (ctypes.c_size_t, [_P]),
     "jmg_solve_fixed_vjp": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(JmgCoeffs), _P, _P, _P, _P, _P, _P, _P,
                                            ctypes.c_size_t, _P, ctypes.c_size_t, _P]),
+    "jmg_net_num_params": (ctypes.c_int64, []),
+    "jmg_net_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int]),
+    "jmg_net_destroy": (None, [_P]),
+    "jmg_net_set_params": (ctypes.c_int, [_P, _P, _P]),
+    "jmg_net_get_params": (ctypes.c_int, [_P, _P, _P]),
+    "jmg_net_forward": (ctypes.c_int, [_P, _P, ctypes.c_int, _P, _P]),
+    "jmg_net_loss_grad": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, _P, _P, _P]),
+    "jmg_net_train_step": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_float, _P, _P]),
+    "jmg_net_inputs_2d": (ctypes.c_int, [_P, ctypes.POINTER(JmgGrid), ctypes.POINTER(JmgCoeffs), _P, _P, _P, _P]),
+    "jmg_net_target_2d": (ctypes.c_int, [_P, ctypes.POINTER(JmgGrid), _P, _P, ctypes.c_float, _P, _P]),
+    "jmg_net_guess_2d": (ctypes.c_int, [_P, ctypes.POINTER(JmgGrid), ctypes.POINTER(JmgCoeffs), _P, ctypes.c_float,
+                                        _P, _P]),
     "jmg_last_error": (ctypes.c_char_p, []),
 }
 

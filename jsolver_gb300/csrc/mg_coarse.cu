@@ -1,178 +1,346 @@
-// mg_coarse.cu — the coarse levels of a cycle inside one thread block, from shared memory.
+// mg_coarse.cu — the coarse levels of a cycle on one thread-block cluster.
 //
-// Below a few thousand points per level, a grid-wide launch per operator costs more in
-// launch latency than in work. k_coarse_smem runs the reference's recursion
-// (solver_2d.py:582-614) for every level from `lev0` down to L-2 in one block of 1024
-// threads. phi and rhs of those levels live in dynamic shared memory in a compact
-// layout (nx * ny * nz per level); the coefficients stay in global memory (they were
-// written before the launch and are only read, through the read-only cache). The block
-// loads phi/rhs of lev0 at entry and writes phi of lev0 back at exit; the deeper levels
-// exist only in shared memory. The arithmetic of every point is the same as in the
-// grid-wide kernels (mg_common.cuh), in the reference's order.
+// Below ~20 000 points per level a grid-wide launch per operator costs more in launch
+// latency than in work, but one SM is too slow for the work itself: GB300 issues about
+// two FP64 FMAs per clock per SM, so a 64^2 level alone keeps a single block busy for
+// tens of microseconds per cycle. k_coarse_cluster runs the reference's recursion
+// (solver_2d.py:582-614, solver_3d.py:587-619) for every level from `lev0` down to L-2
+// on a cluster of R CTAs (16 where the GPU allows it, else 8), one CTA per SM:
+//   * every level's rows (2D: j; 3D: the (k, j) rows) are split into R contiguous
+//     blocks, one per CTA; a CTA keeps phi, rhs and the coefficient arrays (wx, wy, wz,
+//     acc, invd) of its rows in its own shared memory, loaded from global memory at
+//     entry; levels of at most kLocalPoints points live whole in CTA 0;
+//   * a point's neighbours in other CTAs' rows are read through distributed shared
+//     memory (generic pointers from cluster.map_shared_rank);
+//   * passes that touch a spread level end with a cluster barrier (release/acquire),
+//     passes on CTA-0-only levels with a block barrier;
+//   * at exit every CTA writes phi of its rows of `lev0` back to global memory.
+// The arithmetic of every point is that of the grid-wide kernels (mg_common.cuh), in
+// the reference's order, so results are bit-identical to them.
+#include <cooperative_groups.h>
+
 #include "mg_common.cuh"
 #include "mg_kernels.h"
 
+namespace cg = cooperative_groups;
+
 namespace jmg {
 
+namespace {
+
+constexpr int kThreads = 512;
+constexpr int kLocalPoints = 1024;  // levels up to this many padded points live in CTA 0
+
+// array slots of a level block
+enum { A_PHI = 0, A_RHS, A_WX, A_WY, A_ACC, A_INVD, A_WZ };
+
 template <typename T>
-struct SmemView {
-  T* phi;
-  T* rhs;
-  int nx, ny, nz;  // compact padded extents
+struct Ctx {
+  T* sm;                 // this CTA's shared memory
+  T* const* rb;          // generic pointers to every CTA's shared memory (rank-indexed)
+  int me;
 };
 
+// one level as seen from one CTA. Row s of array a of the level sits in the CTA that
+// owns s at element off + (a * rpr + ls) * rp, ls = s - first row of that CTA.
 template <typename T, int DIM>
-__device__ __forceinline__ T s_gs(const SmemView<T>& v, const Lvl<T>& g, int k, int j, int i) {
-  const int sy = v.nx, sz = v.nx * v.ny;
-  const int q = (k * v.ny + j) * v.nx + i;
-  const long long p = (long long)k * g.S + (long long)j * g.P + i;
-  const T* ph = v.phi;
+struct DLevel {
+  int off, nx, ny, rp, nrows, rpr, dist, as;
+  int mx, my, mz;
+  int s0, s1;  // rows owned by this CTA ([0, 0) for none)
+
+  __device__ void init(const ClusterLevel& L, int me) {
+    off = L.off;
+    nx = L.nx;
+    ny = L.ny;
+    rp = L.rp;
+    nrows = L.nrows;
+    rpr = L.rpr;
+    dist = L.dist;
+    as = rpr * rp;
+    mx = L.m[0];
+    my = L.m[1];
+    mz = L.m[2];
+    if (dist) {
+      s0 = min(nrows, me * rpr);
+      s1 = min(nrows, s0 + rpr);
+    } else {
+      s0 = 0;
+      s1 = me == 0 ? nrows : 0;
+    }
+  }
+  // array-0 (phi) pointer of row s, wherever it lives; array a is at + a * as
+  __device__ __forceinline__ T* rowp(const Ctx<T>& c, int s) const {
+    if (!dist) return c.sm + off + s * rp;
+    if (s >= s0 && s < s0 + rpr) return c.sm + off + (s - s0) * rp;
+    const int r = s / rpr;
+    return c.rb[r] + off + (s - r * rpr) * rp;
+  }
+  // owned row (local)
+  __device__ __forceinline__ T* own(const Ctx<T>& c, int s) const { return c.sm + off + (s - s0) * rp; }
+};
+
+// ---- point arithmetic on distributed rows (same order as mg_common.cuh) -----------------
+// q: the point's row, qn / qs: rows j+1 / j-1, qu / qd: rows k+1 / k-1 (3D); arrays at
+// multiples of `as`.
+
+template <typename T, int DIM>
+__device__ __forceinline__ T d_gs(const T* q, const T* qn, const T* qs, const T* qu, const T* qd, int as, int i) {
   T s;
   if (DIM == 3) {
-    s = __ldg(&g.wz[p]) * ph[q + sz];
-    s = fma(__ldg(&g.wz[p - g.S]), ph[q - sz], s);
-    s = fma(__ldg(&g.wy[p]), ph[q + sy], s);
+    s = q[A_WZ * as + i] * qu[i];
+    s = fma(qd[A_WZ * as + i], qd[i], s);
+    s = fma(q[A_WY * as + i], qn[i], s);
   } else {
-    s = __ldg(&g.wy[p]) * ph[q + sy];
+    s = q[A_WY * as + i] * qn[i];
   }
-  s = fma(__ldg(&g.wy[p - g.P]), ph[q - sy], s);
-  s = fma(__ldg(&g.wx[p]), ph[q + 1], s);
-  s = fma(__ldg(&g.wx[p - 1]), ph[q - 1], s);
-  s = s - v.rhs[q];
-  return s * __ldg(&g.invd[p]);
+  s = fma(qs[A_WY * as + i], qs[i], s);
+  s = fma(q[A_WX * as + i], q[i + 1], s);
+  s = fma(q[A_WX * as + i - 1], q[i - 1], s);
+  s = s - q[A_RHS * as + i];
+  return s * q[A_INVD * as + i];
 }
 
 template <typename T, int DIM>
-__device__ __forceinline__ T s_defect(const SmemView<T>& v, const Lvl<T>& g, int k, int j, int i) {
-  const int sy = v.nx, sz = v.nx * v.ny;
-  const int q = (k * v.ny + j) * v.nx + i;
-  const long long p = (long long)k * g.S + (long long)j * g.P + i;
-  const T* ph = v.phi;
-  T d = __ldg(&g.acc[p]) * ph[q];
-  d = fma(-__ldg(&g.wx[p - 1]), ph[q - 1], d);
-  d = fma(-__ldg(&g.wx[p]), ph[q + 1], d);
-  d = fma(-__ldg(&g.wy[p - g.P]), ph[q - sy], d);
-  d = fma(-__ldg(&g.wy[p]), ph[q + sy], d);
+__device__ __forceinline__ T d_defect(const T* q, const T* qn, const T* qs, const T* qu, const T* qd, int as, int i) {
+  T d = q[A_ACC * as + i] * q[i];
+  d = fma(-q[A_WX * as + i - 1], q[i - 1], d);
+  d = fma(-q[A_WX * as + i], q[i + 1], d);
+  d = fma(-qs[A_WY * as + i], qs[i], d);
+  d = fma(-q[A_WY * as + i], qn[i], d);
   if (DIM == 3) {
-    d = fma(-__ldg(&g.wz[p - g.S]), ph[q - sz], d);
-    d = fma(-__ldg(&g.wz[p]), ph[q + sz], d);
+    d = fma(-qd[A_WZ * as + i], qd[i], d);
+    d = fma(-q[A_WZ * as + i], qu[i], d);
   }
-  return d + v.rhs[q];
+  return d + q[A_RHS * as + i];
+}
+
+// defect at fine (k, j, i), looking its rows up
+template <typename T, int DIM>
+__device__ __forceinline__ T d_defect_at(const Ctx<T>& c, const DLevel<T, DIM>& f, int k, int j, int i) {
+  const int s = k * f.ny + j;
+  const T* q = f.rowp(c, s);
+  const T* qn = f.rowp(c, s + 1);
+  const T* qs = f.rowp(c, s - 1);
+  const T* qu = DIM == 3 ? f.rowp(c, s + f.ny) : nullptr;
+  const T* qd = DIM == 3 ? f.rowp(c, s - f.ny) : nullptr;
+  return d_defect<T, DIM>(q, qn, qs, qu, qd, f.as, i);
 }
 
 template <typename T, int DIM>
-__device__ void s_sweep(const SmemView<T>& v, const Lvl<T>& g) {
-  const int hx = g.mx / 2, ny = g.my - 1, nz = DIM == 3 ? g.mz - 1 : 1;
-  const int n = hx * ny * nz;
-  for (int color = 0; color < 2; ++color) {
-    const int par = DIM == 2 ? color : (first_color_parity<3>() + color) & 1;
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-      const int r = t / hx;
-      const int j = 2 + r % ny, k = DIM == 3 ? 2 + r / ny : 0;
-      const int i = 2 + ((j + k + par) & 1) + 2 * (t % hx);
-      if (i > g.mx) continue;
-      v.phi[(k * v.ny + j) * v.nx + i] = s_gs<T, DIM>(v, g, k, j, i);
+__device__ __forceinline__ T d_restrict(const Ctx<T>& c, const DLevel<T, DIM>& f, int K, int J, int I) {
+  const int i = 2 * I - 1, j = 2 * J - 1;
+  if constexpr (DIM == 2) {
+    // fine rows j-2 .. j+2
+    const T* r0 = f.rowp(c, j - 2);
+    const T* r1 = f.rowp(c, j - 1);
+    const T* r2 = f.rowp(c, j);
+    const T* r3 = f.rowp(c, j + 1);
+    const T* r4 = f.rowp(c, j + 2);
+    const int as = f.as;
+    const T dne = d_defect<T, 2>(r3, r4, r2, nullptr, nullptr, as, i + 1);
+    const T dnw = d_defect<T, 2>(r3, r4, r2, nullptr, nullptr, as, i - 1);
+    const T dse = d_defect<T, 2>(r1, r2, r0, nullptr, nullptr, as, i + 1);
+    const T dsw = d_defect<T, 2>(r1, r2, r0, nullptr, nullptr, as, i - 1);
+    const T dc = d_defect<T, 2>(r2, r3, r1, nullptr, nullptr, as, i);
+    return T(0.0625) * (((dne + dnw) + dse) + dsw) + T(0.25) * dc;
+  } else {
+    const int k = 2 * K - 1;
+    T s = d_defect_at<T, 3>(c, f, k, j + 1, i + 1);
+    s = s + d_defect_at<T, 3>(c, f, k, j + 1, i - 1);
+    s = s + d_defect_at<T, 3>(c, f, k, j - 1, i + 1);
+    s = s + d_defect_at<T, 3>(c, f, k, j - 1, i - 1);
+    s = s + d_defect_at<T, 3>(c, f, k + 1, j, i + 1);
+    s = s + d_defect_at<T, 3>(c, f, k + 1, j, i - 1);
+    s = s + d_defect_at<T, 3>(c, f, k - 1, j, i + 1);
+    s = s + d_defect_at<T, 3>(c, f, k - 1, j, i - 1);
+    s = s + d_defect_at<T, 3>(c, f, k + 1, j + 1, i);
+    s = s + d_defect_at<T, 3>(c, f, k + 1, j - 1, i);
+    s = s + d_defect_at<T, 3>(c, f, k - 1, j + 1, i);
+    s = s + d_defect_at<T, 3>(c, f, k - 1, j - 1, i);
+    return T(0.03125) * s + T(0.125) * d_defect_at<T, 3>(c, f, k, j, i);
+  }
+}
+
+// prolongated correction at fine (k, j, i) from the coarse level (prolong_point2d/3d)
+template <typename T, int DIM>
+__device__ __forceinline__ bool d_prolong(const Ctx<T>& c, const DLevel<T, DIM>& cv, int k, int j, int i,
+                                          bool diag, T* out) {
+  if constexpr (DIM == 2) {
+    const bool jo = j & 1, io = i & 1;
+    if (jo && io) {
+      *out = cv.rowp(c, (j + 1) >> 1)[(i + 1) >> 1];
+    } else if (jo) {
+      const T* r = cv.rowp(c, (j + 1) >> 1);
+      *out = T(0.5) * (r[(i + 2) >> 1] + r[i >> 1]);
+    } else if (io) {
+      const int ci = (i + 1) >> 1;
+      *out = T(0.5) * (cv.rowp(c, (j + 2) >> 1)[ci] + cv.rowp(c, j >> 1)[ci]);
+    } else {
+      if (!diag) return false;
+      const T* rp = cv.rowp(c, (j + 2) >> 1);
+      const T* rm = cv.rowp(c, j >> 1);
+      const int cp = (i + 2) >> 1, cm = i >> 1;
+      *out = T(0.25) * (((rp[cp] + rm[cp]) + rp[cm]) + rm[cm]);
     }
-    __syncthreads();
+    return true;
+  } else {
+    auto C = [&](int K, int J, int I) -> T { return cv.rowp(c, K * cv.ny + J)[I]; };
+    const int ke = !(k & 1), je = !(j & 1), ie = !(i & 1);
+    const int ne = ke + je + ie;
+    const int kp = ke ? (k + 2) >> 1 : (k + 1) >> 1, km = ke ? (k >> 1) : kp;
+    const int jp = je ? (j + 2) >> 1 : (j + 1) >> 1, jm = je ? (j >> 1) : jp;
+    const int ip = ie ? (i + 2) >> 1 : (i + 1) >> 1, im = ie ? (i >> 1) : ip;
+    if (ne == 0) {
+      *out = C(kp, jp, ip);
+    } else if (ne == 1) {
+      if (ie) *out = T(0.5) * (C(kp, jp, ip) + C(kp, jp, im));
+      else if (je) *out = T(0.5) * (C(kp, jp, ip) + C(kp, jm, ip));
+      else *out = T(0.5) * (C(kp, jp, ip) + C(km, jp, ip));
+    } else if (ne == 2) {
+      if (!diag) return false;
+      if (!ke) *out = T(0.25) * (((C(kp, jp, ip) + C(kp, jm, ip)) + C(kp, jp, im)) + C(kp, jm, im));
+      else if (!je) *out = T(0.25) * (((C(kp, jp, ip) + C(km, jp, ip)) + C(kp, jp, im)) + C(km, jp, im));
+      else *out = T(0.25) * (((C(kp, jp, ip) + C(km, jp, ip)) + C(kp, jm, ip)) + C(km, jm, ip));
+    } else {
+      T s = C(kp, jp, ip);
+      s = s + C(km, jp, ip);
+      s = s + C(kp, jm, ip);
+      s = s + C(km, jm, ip);
+      s = s + C(kp, jp, im);
+      s = s + C(km, jp, im);
+      s = s + C(kp, jm, im);
+      s = s + C(km, jm, im);
+      *out = T(0.125) * s;
+    }
+    return true;
+  }
+}
+
+// ---- passes ------------------------------------------------------------------------------
+
+template <typename T, int DIM>
+__device__ __forceinline__ bool interior_row(const DLevel<T, DIM>& v, int s, int* k, int* j) {
+  *k = DIM == 3 ? s / v.ny : 0;
+  *j = DIM == 3 ? s - *k * v.ny : s;
+  return *j >= 2 && *j <= v.my && (DIM == 2 || (*k >= 2 && *k <= v.mz));
+}
+
+template <typename T, int DIM>
+__device__ void p_sweep_colour(const Ctx<T>& c, const DLevel<T, DIM>& v, int colour) {
+  const int par = DIM == 2 ? colour : (first_color_parity<3>() + colour) & 1;
+  const int hx = v.mx / 2;
+  const int n = (v.s1 - v.s0) * hx;
+  for (int t = threadIdx.x; t < n; t += kThreads) {
+    const int q = t / hx;
+    const int s = v.s0 + q;
+    int k, j;
+    if (!interior_row(v, s, &k, &j)) continue;
+    const int i = 2 + ((j + k + par) & 1) + 2 * (t - q * hx);
+    if (i > v.mx) continue;
+    T* r = v.own(c, s);
+    const T* rn = v.rowp(c, s + 1);
+    const T* rs = v.rowp(c, s - 1);
+    const T* ru = DIM == 3 ? v.rowp(c, s + v.ny) : nullptr;
+    const T* rd = DIM == 3 ? v.rowp(c, s - v.ny) : nullptr;
+    r[i] = d_gs<T, DIM>(r, rn, rs, ru, rd, v.as, i);
   }
 }
 
 template <typename T, int DIM>
-__device__ void s_restrict(const SmemView<T>& f, const Lvl<T>& gf, const SmemView<T>& c, const Lvl<T>& gc) {
-  const int n = c.nx * c.ny * c.nz;
-  for (int t = threadIdx.x; t < n; t += blockDim.x) {
-    const int I = t % c.nx, J = (t / c.nx) % c.ny, K = t / (c.nx * c.ny);
-    T v = T(0);
-    const bool in = I >= 2 && I <= gc.mx && J >= 2 && J <= gc.my && (DIM == 2 || (K >= 2 && K <= gc.mz));
-    if (in) {
-      const int i = 2 * I - 1, j = 2 * J - 1, k = DIM == 3 ? 2 * K - 1 : 0;
-      if (DIM == 2) {
-        const T dne = s_defect<T, 2>(f, gf, 0, j + 1, i + 1);
-        const T dnw = s_defect<T, 2>(f, gf, 0, j + 1, i - 1);
-        const T dse = s_defect<T, 2>(f, gf, 0, j - 1, i + 1);
-        const T dsw = s_defect<T, 2>(f, gf, 0, j - 1, i - 1);
-        const T dc = s_defect<T, 2>(f, gf, 0, j, i);
-        v = T(0.0625) * (((dne + dnw) + dse) + dsw) + T(0.25) * dc;
-      } else {
-        // the 12 edge-diagonal red neighbours in the reference's order (solver_3d.py:649)
-        T s = s_defect<T, 3>(f, gf, k, j + 1, i + 1);
-        s = s + s_defect<T, 3>(f, gf, k, j + 1, i - 1);
-        s = s + s_defect<T, 3>(f, gf, k, j - 1, i + 1);
-        s = s + s_defect<T, 3>(f, gf, k, j - 1, i - 1);
-        s = s + s_defect<T, 3>(f, gf, k + 1, j, i + 1);
-        s = s + s_defect<T, 3>(f, gf, k + 1, j, i - 1);
-        s = s + s_defect<T, 3>(f, gf, k - 1, j, i + 1);
-        s = s + s_defect<T, 3>(f, gf, k - 1, j, i - 1);
-        s = s + s_defect<T, 3>(f, gf, k + 1, j + 1, i);
-        s = s + s_defect<T, 3>(f, gf, k + 1, j - 1, i);
-        s = s + s_defect<T, 3>(f, gf, k - 1, j + 1, i);
-        s = s + s_defect<T, 3>(f, gf, k - 1, j - 1, i);
-        v = T(0.03125) * s + T(0.125) * s_defect<T, 3>(f, gf, k, j, i);
+__device__ void p_restrict(const Ctx<T>& c, const DLevel<T, DIM>& f, const DLevel<T, DIM>& cv) {
+  const int n = (cv.s1 - cv.s0) * cv.nx;
+  for (int t = threadIdx.x; t < n; t += kThreads) {
+    const int q = t / cv.nx, I = t - q * cv.nx;
+    const int s = cv.s0 + q;
+    int K, J;
+    T val = T(0);
+    if (interior_row(cv, s, &K, &J) && I >= 2 && I <= cv.mx) val = d_restrict<T, DIM>(c, f, K, J, I);
+    T* r = cv.own(c, s);
+    r[A_RHS * cv.as + I] = val;
+    r[I] = T(0);
+  }
+}
+
+template <typename T, int DIM>
+__device__ void p_prolong(const Ctx<T>& c, const DLevel<T, DIM>& f, const DLevel<T, DIM>& cv, bool diag) {
+  const int nx = f.mx - 1;
+  const int n = (f.s1 - f.s0) * nx;
+  for (int t = threadIdx.x; t < n; t += kThreads) {
+    const int q = t / nx, i = 2 + (t - q * nx);
+    int k, j;
+    if (!interior_row(f, f.s0 + q, &k, &j)) continue;
+    T val;
+    if (d_prolong<T, DIM>(c, cv, k, j, i, diag, &val)) {
+      T* ph = f.own(c, f.s0 + q);
+      ph[i] = ph[i] + val;
+    }
+  }
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)),
+               "l"(gmem));
+}
+
+template <typename T, int DIM>
+__global__ void __launch_bounds__(kThreads) k_coarse_cluster(const LvlTable<T>* __restrict__ tab, ClusterLayout lay,
+                                                             CycleParams cp, int fcycle0, int skip_pre0) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T* rb[kMaxClusterRanks];
+  cg::cluster_group cluster = cg::this_cluster();
+  Ctx<T> c;
+  c.sm = reinterpret_cast<T*>(smem_raw);
+  c.rb = rb;
+  c.me = (int)cluster.block_rank();
+  if (threadIdx.x < lay.ranks) rb[threadIdx.x] = cluster.map_shared_rank(c.sm, (int)threadIdx.x);
+  const int lev0 = lay.lev0;
+
+  // stage the owned rows in shared memory with 16-byte asynchronous copies: the
+  // coefficients of every level, phi and rhs of the entry level. A global row starts on
+  // a 128-byte boundary and its pitch covers the copied rp >= nx elements.
+  constexpr int kV = 16 / sizeof(T);  // elements per copy
+  for (int l = lev0; l <= lay.last; ++l) {
+    DLevel<T, DIM> v;
+    v.init(lay.l[l - lev0], c.me);
+    const Lvl<T>& g = tab->l[l];
+    const int cpr = v.rp / kV;  // copies per row
+    const int n = (v.s1 - v.s0) * cpr;
+    const int na = DIM == 3 ? 7 : 6;
+    for (int a = l == lev0 ? A_PHI : A_WX; a < na; ++a) {
+      const T* src = a == A_PHI ? g.phi : a == A_RHS ? g.rhs : a == A_WX ? g.wx : a == A_WY ? g.wy
+                   : a == A_ACC ? g.acc : a == A_INVD ? g.invd : g.wz;
+      T* dst = c.sm + v.off + a * v.as;
+      for (int t = threadIdx.x; t < n; t += kThreads) {
+        const int q = t / cpr, e = (t - q * cpr) * kV;
+        const int s = v.s0 + q;
+        const int k = DIM == 3 ? s / v.ny : 0, j = s - k * v.ny;
+        cp_async16(dst + q * v.rp + e, src + (long long)k * g.S + (long long)j * g.P + e);
       }
     }
-    c.rhs[t] = v;
-    c.phi[t] = T(0);
   }
-  __syncthreads();
-}
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  cluster.sync();
 
-template <typename T, int DIM>
-__device__ void s_prolong(const SmemView<T>& f, const Lvl<T>& gf, const SmemView<T>& c, bool diag) {
-  // the coarse values are read through a Lvl view of the compact smem layout
-  Lvl<T> cv;
-  cv.phi = c.phi;
-  cv.P = c.nx;
-  cv.S = (long long)c.nx * c.ny;
-  const int nx = gf.mx - 1, ny = gf.my - 1, nz = DIM == 3 ? gf.mz - 1 : 1;
-  const int n = nx * ny * nz;
-  for (int t = threadIdx.x; t < n; t += blockDim.x) {
-    const int i = 2 + t % nx, j = 2 + (t / nx) % ny, k = DIM == 3 ? 2 + t / (nx * ny) : 0;
-    T v;
-    const bool ok = DIM == 2 ? prolong_point2d<T>(cv, j, i, diag, &v) : prolong_point3d<T>(cv, k, j, i, diag, &v);
-    if (ok) {
-      const int q = (k * f.ny + j) * f.nx + i;
-      f.phi[q] = f.phi[q] + v;
+  // pass bookkeeping: a pass on a spread level, or one following a CTA-0-only pass that
+  // the next pass reads remotely, is fenced by cluster barriers
+  bool prev_local = false;
+  auto begin = [&](bool spread) {
+    if (spread && prev_local) cluster.sync();
+  };
+  auto end = [&](bool spread) {
+    if (spread) cluster.sync();
+    else __syncthreads();
+    prev_local = !spread;
+  };
+  auto sweep = [&](const DLevel<T, DIM>& v) {
+    for (int colour = 0; colour < 2; ++colour) {
+      begin(v.dist);
+      if (v.s1 > v.s0) p_sweep_colour<T, DIM>(c, v, colour);
+      end(v.dist);
     }
-  }
-  __syncthreads();
-}
+  };
 
-// shared-memory view of level l: levels lev0..l-1 come first, phi then rhs each
-template <typename T, int DIM>
-__device__ __forceinline__ SmemView<T> view_of(const LvlTable<T>* tab, T* base, int lev0, int l) {
-  int off = 0;
-  for (int k = lev0; k < l; ++k) {
-    const Lvl<T>& g = tab->l[k];
-    off += 2 * (g.mx + 3) * (g.my + 3) * (DIM == 3 ? g.mz + 3 : 1);
-  }
-  const Lvl<T>& g = tab->l[l];
-  SmemView<T> v;
-  v.nx = g.mx + 3;
-  v.ny = g.my + 3;
-  v.nz = DIM == 3 ? g.mz + 3 : 1;
-  v.phi = base + off;
-  v.rhs = base + off + v.nx * v.ny * v.nz;
-  return v;
-}
-
-template <typename T, int DIM>
-__global__ void __launch_bounds__(1024) k_coarse_smem(const LvlTable<T>* __restrict__ tab, CycleParams cp,
-                                                      int lev0, int fcycle0, int skip_pre0) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* base = reinterpret_cast<T*>(smem_raw);
-  // load phi and rhs of the entry level
-  {
-    const Lvl<T>& g = tab->l[lev0];
-    const SmemView<T> v0 = view_of<T, DIM>(tab, base, lev0, lev0);
-    const int n = v0.nx * v0.ny * v0.nz;
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-      const int I = t % v0.nx, J = (t / v0.nx) % v0.ny, K = t / (v0.nx * v0.ny);
-      const long long p = (long long)K * g.S + (long long)J * g.P + I;
-      v0.phi[t] = g.phi[p];
-      v0.rhs[t] = g.rhs[p];
-    }
-    __syncthreads();
-  }
   struct Frame {
     int lev, stage, g;
     bool fcycle, skip_pre;
@@ -181,88 +349,147 @@ __global__ void __launch_bounds__(1024) k_coarse_smem(const LvlTable<T>* __restr
   int sp = 0;
   st[sp++] = Frame{lev0, 0, 0, fcycle0 != 0, skip_pre0 != 0};
   while (sp > 0) {
-    Frame& f = st[sp - 1];
-    const Lvl<T>& g = tab->l[f.lev];
-    const SmemView<T> vf = view_of<T, DIM>(tab, base, lev0, f.lev);
-    if (f.lev == cp.last_level) {
-      for (int s = 0; s < cp.nu1 + cp.nu2; ++s) s_sweep<T, DIM>(vf, g);
+    Frame& fr = st[sp - 1];
+    DLevel<T, DIM> vf;
+    vf.init(lay.l[fr.lev - lev0], c.me);
+    if (fr.lev == cp.last_level) {
+      for (int s = 0; s < cp.nu1 + cp.nu2; ++s) sweep(vf);
       --sp;
       continue;
     }
-    const SmemView<T> vc = view_of<T, DIM>(tab, base, lev0, f.lev + 1);
-    if (f.stage == 0) {
-      if (!f.skip_pre)
-        for (int s = 0; s < cp.nu1; ++s) s_sweep<T, DIM>(vf, g);
-      s_restrict<T, DIM>(vf, g, vc, tab->l[f.lev + 1]);
-      f.stage = f.fcycle ? 1 : 2;
-      f.g = 0;
+    DLevel<T, DIM> vc;
+    vc.init(lay.l[fr.lev + 1 - lev0], c.me);
+    const bool spread = vf.dist || vc.dist;
+    if (fr.stage == 0) {
+      if (!fr.skip_pre)
+        for (int s = 0; s < cp.nu1; ++s) sweep(vf);
+      begin(spread);
+      if (vc.s1 > vc.s0) p_restrict<T, DIM>(c, vf, vc);
+      end(spread);
+      fr.stage = fr.fcycle ? 1 : 2;
+      fr.g = 0;
     }
-    if (f.stage == 1) {
-      if (f.g < cp.gamma) {
-        ++f.g;
-        st[sp++] = Frame{f.lev + 1, 0, 0, true, false};
+    if (fr.stage == 1) {
+      if (fr.g < cp.gamma) {
+        ++fr.g;
+        st[sp++] = Frame{fr.lev + 1, 0, 0, true, false};
         continue;
       }
-      f.stage = 2;
-      f.g = 0;
+      fr.stage = 2;
+      fr.g = 0;
     }
-    if (f.stage == 2) {
-      if (f.g < cp.gamma) {
-        ++f.g;
-        st[sp++] = Frame{f.lev + 1, 0, 0, false, false};
+    if (fr.stage == 2) {
+      if (fr.g < cp.gamma) {
+        ++fr.g;
+        st[sp++] = Frame{fr.lev + 1, 0, 0, false, false};
         continue;
       }
-      f.stage = 3;
+      fr.stage = 3;
     }
-    s_prolong<T, DIM>(vf, g, vc, cp.diag != 0);
-    for (int s = 0; s < cp.nu2; ++s) s_sweep<T, DIM>(vf, g);
+    begin(spread);
+    if (vf.s1 > vf.s0) p_prolong<T, DIM>(c, vf, vc, cp.diag != 0);
+    end(spread);
+    for (int s = 0; s < cp.nu2; ++s) sweep(vf);
     --sp;
   }
-  // write phi of the entry level back
+
+  // write phi of the owned rows of the entry level back
   {
+    DLevel<T, DIM> v;
+    v.init(lay.l[0], c.me);
     const Lvl<T>& g = tab->l[lev0];
-    const SmemView<T> v0 = view_of<T, DIM>(tab, base, lev0, lev0);
-    const int n = v0.nx * v0.ny * v0.nz;
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-      const int I = t % v0.nx, J = (t / v0.nx) % v0.ny, K = t / (v0.nx * v0.ny);
-      g.phi[(long long)K * g.S + (long long)J * g.P + I] = v0.phi[t];
+    const int n = (v.s1 - v.s0) * v.nx;
+    for (int t = threadIdx.x; t < n; t += kThreads) {
+      const int q = t / v.nx, i = t - q * v.nx;
+      const int s = v.s0 + q;
+      const int k = DIM == 3 ? s / v.ny : 0, j = s - k * v.ny;
+      g.phi[(long long)k * g.S + (long long)j * g.P + i] = c.sm[v.off + q * v.rp + i];
     }
   }
+  // no CTA leaves while another may still read its shared memory
+  cluster.sync();
 }
 
-size_t coarse_smem_bytes(int dim, const int* m0, int lev0, int last, size_t elem) {
-  size_t n = 0;
+}  // namespace
+
+int cluster_layout(int dim, const int m[][3], int lev0, int last, int ranks, ClusterLayout* out) {
+  if (last - lev0 + 1 > kMaxLevels || ranks > kMaxClusterRanks || ranks < 1) return 1;
+  ClusterLayout& lay = *out;
+  lay.lev0 = lev0;
+  lay.last = last;
+  lay.ranks = ranks;
+  const int na = dim == 3 ? 7 : 6;
+  long long off = 0;
   for (int l = lev0; l <= last; ++l) {
-    size_t e = (size_t)((m0[0] >> l) + 3) * ((m0[1] >> l) + 3);
-    if (dim == 3) e *= (size_t)((m0[2] >> l) + 3);
-    n += 2 * e;
+    ClusterLevel& L = lay.l[l - lev0];
+    L.m[0] = m[l][0];
+    L.m[1] = m[l][1];
+    L.m[2] = dim == 3 ? m[l][2] : 0;
+    L.nx = m[l][0] + 3;
+    L.ny = m[l][1] + 3;
+    L.rp = (L.nx + 3) & ~3;  // row pitch: 16-byte rows for either element size
+    const int nz = dim == 3 ? m[l][2] + 3 : 1;
+    L.nrows = L.ny * nz;
+    L.dist = (long long)L.nx * L.nrows > kLocalPoints && ranks > 1;
+    L.rpr = L.dist ? (L.nrows + ranks - 1) / ranks : L.nrows;
+    L.off = (int)off;
+    off += (long long)na * L.rpr * L.rp;
   }
-  return n * elem;
+  lay.elems = off;
+  return 0;
 }
 
 template <typename T>
-int prepare_coarse_smem(int dim, size_t bytes) {
-  cudaError_t e = dim == 2 ? cudaFuncSetAttribute(k_coarse_smem<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  (int)bytes)
-                           : cudaFuncSetAttribute(k_coarse_smem<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  (int)bytes);
-  return e == cudaSuccess ? 0 : 1;
+int prepare_coarse_cluster(int dim, size_t smem_bytes, int ranks) {
+  const void* fn = dim == 2 ? (const void*)k_coarse_cluster<T, 2> : (const void*)k_coarse_cluster<T, 3>;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes) != cudaSuccess) return 1;
+  if (ranks > 8 && cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+    return 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(ranks);
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = smem_bytes;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = ranks;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int nclusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return nclusters >= 1 ? 0 : 1;
 }
 
 template <typename T>
-void launch_coarse_smem(int dim, const LvlTable<T>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
-                        size_t smem, cudaStream_t s) {
+void launch_coarse_cluster(int dim, const LvlTable<T>* tab, const ClusterLayout& lay, const CycleParams& cp,
+                           int fcycle, int skip_pre, size_t smem_bytes, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(lay.ranks);
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = smem_bytes;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = lay.ranks;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
   if (dim == 2)
-    k_coarse_smem<T, 2><<<1, 1024, smem, s>>>(tab, cp, lev, fcycle, skip_pre);
+    cudaLaunchKernelEx(&cfg, k_coarse_cluster<T, 2>, tab, lay, cp, fcycle, skip_pre);
   else
-    k_coarse_smem<T, 3><<<1, 1024, smem, s>>>(tab, cp, lev, fcycle, skip_pre);
+    cudaLaunchKernelEx(&cfg, k_coarse_cluster<T, 3>, tab, lay, cp, fcycle, skip_pre);
 }
 
-template int prepare_coarse_smem<double>(int, size_t);
-template int prepare_coarse_smem<float>(int, size_t);
-template void launch_coarse_smem<double>(int, const LvlTable<double>*, const CycleParams&, int, int, int, size_t,
-                                         cudaStream_t);
-template void launch_coarse_smem<float>(int, const LvlTable<float>*, const CycleParams&, int, int, int, size_t,
-                                        cudaStream_t);
+template int prepare_coarse_cluster<double>(int, size_t, int);
+template int prepare_coarse_cluster<float>(int, size_t, int);
+template void launch_coarse_cluster<double>(int, const LvlTable<double>*, const ClusterLayout&, const CycleParams&,
+                                            int, int, size_t, cudaStream_t);
+template void launch_coarse_cluster<float>(int, const LvlTable<float>*, const ClusterLayout&, const CycleParams&, int,
+                                           int, size_t, cudaStream_t);
 
 }  // namespace jmg

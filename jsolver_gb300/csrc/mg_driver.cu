@@ -48,6 +48,16 @@ int set_err(int code, const char* fmt, ...) {
     if (e_ != cudaSuccess) return set_err(JMG_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
   } while (0)
 
+// First level run by the single-block global-memory coarse kernel: at most 8192 padded
+// points, and never below the last visited level.
+int block_coarse_start(const JmgPlan* p) {
+  for (int l = 0; l < p->used; ++l) {
+    const long long pts = (long long)p->lv[l].box.nx * p->lv[l].box.ny * p->lv[l].box.nz;
+    if (pts <= 8192) return l;
+  }
+  return p->used - 1;
+}
+
 int validate_and_layout(JmgPlan* p) {
   const JmgGrid& g = p->grid;
   if (g.ndim != 2 && g.ndim != 3) return set_err(JMG_ERR_VALUE, "ndim must be 2 or 3, got %d", g.ndim);
@@ -130,22 +140,12 @@ int validate_and_layout(JmgPlan* p) {
   p->off_tab64 = take(sizeof(LvlTable<double>));
   p->off_tab32 = take(sizeof(LvlTable<float>));
   p->ws_bytes = off;
-  // coarse levels: at most 8192 padded points, and never below the last visited level
-  int cs = p->used - 1;
-  for (int l = 0; l < p->used; ++l) {
-    const long long pts = (long long)p->lv[l].box.nx * p->lv[l].box.ny * p->lv[l].box.nz;
-    if (pts <= 8192) {
-      cs = l;
-      break;
-    }
-  }
-  p->coarse_start = cs;
+  // the coarse levels are chosen at the first solve (coarse_setup), when the GPU's
+  // cluster support is known; until then the single-block rule holds
+  p->coarse_start = block_coarse_start(p);
   {
-    const int m0[3] = {g.m[0], g.m[1], d == 3 ? g.m[2] : 0};
-    const size_t limit = 200 * 1024;
-    const size_t b64 = coarse_smem_bytes(d, m0, cs, L - 2, 8), b32 = coarse_smem_bytes(d, m0, cs, L - 2, 4);
-    p->coarse_smem64 = b64 <= limit ? b64 : 0;
-    p->coarse_smem32 = b32 <= limit ? b32 : 0;
+    const char* cm = getenv("JMG_COARSE");
+    p->force_block = cm && std::strcmp(cm, "block") == 0;
   }
   const char* hl = getenv("JMG_HOST_LOOP");
   p->host_loop = hl && hl[0] == '1';
@@ -154,6 +154,49 @@ int validate_and_layout(JmgPlan* p) {
 
 
 }  // namespace
+// How the coarse levels of a cycle run. A thread-block cluster of 16 CTAs (8 where 16
+// is not allowed) takes every level from the first one of at most 20 000 padded points
+// whose rows, with the levels below, fit in 200 KB of shared memory per CTA; without
+// cluster support one block runs the levels of at most 8192 points from global memory.
+int jmg::coarse_setup(JmgPlan* p) {
+  if (p->coarse_ready) return JMG_OK;
+  const int last = p->used - 1;
+  const int dim = p->dim;
+  int m[kMaxLevels][3];
+  for (int l = 0; l < p->used && l < kMaxLevels; ++l)
+    for (int a = 0; a < 3; ++a) m[l][a] = p->lv[l].m[a];
+  const size_t limit = 200 * 1024;
+  p->cluster_ranks = 0;
+  p->coarse_start = block_coarse_start(p);
+  if (!p->force_block && p->used <= kMaxLevels) {
+    for (int ranks : {16, 8}) {
+      int lev0 = -1;
+      ClusterLayout lay;
+      for (int l = 0; l <= last; ++l) {
+        const long long pts = (long long)p->lv[l].box.nx * p->lv[l].box.ny * p->lv[l].box.nz;
+        if (pts > 20000) continue;
+        if (cluster_layout(dim, m, l, last, ranks, &lay)) continue;
+        if ((size_t)lay.elems * 8 > limit) continue;
+        lev0 = l;
+        break;
+      }
+      if (lev0 < 0) continue;
+      const size_t b64 = (size_t)lay.elems * 8, b32 = (size_t)lay.elems * 4;
+      if (prepare_coarse_cluster<double>(dim, b64, ranks)) continue;
+      if (p->mixed && prepare_coarse_cluster<float>(dim, b32, ranks)) continue;
+      p->cluster = lay;
+      p->cluster_ranks = ranks;
+      p->cluster_smem64 = b64;
+      p->cluster_smem32 = b32;
+      p->coarse_start = lev0;
+      break;
+    }
+  }
+  cudaGetLastError();  // a refused attribute or occupancy query leaves no sticky error
+  p->coarse_ready = true;
+  return JMG_OK;
+}
+
 Lvl<double> jmg::lvl64(const JmgPlan* p, void* ws, int l) {
   const LevelInfo& li = p->lv[l];
   Lvl<double> a;
@@ -244,9 +287,10 @@ void emit_cycle(const JmgPlan* p, LvlTable<T>& tab, const LvlTable<T>* dtab, con
     else launch_sweep<T>(dim, tab.l[lev], s, top && top->zero_first && first);
   };
   if (lev >= p->coarse_start) {
-    const size_t smem = sizeof(T) == 8 ? p->coarse_smem64 : p->coarse_smem32;
     if (count) *count += 1;
-    else if (smem) launch_coarse_smem<T>(dim, dtab, cp, lev, fcycle ? 1 : 0, skip_pre ? 1 : 0, smem, s);
+    else if (p->cluster_ranks)
+      launch_coarse_cluster<T>(dim, dtab, p->cluster, cp, fcycle ? 1 : 0, skip_pre ? 1 : 0,
+                               sizeof(T) == 8 ? p->cluster_smem64 : p->cluster_smem32, s);
     else launch_coarse_cycle<T>(dim, dtab, cp, lev, fcycle ? 1 : 0, skip_pre ? 1 : 0, s);
     return;
   }
@@ -566,6 +610,7 @@ int jmg_solve(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs
   if (rc) return rc;
   if ((rc = check_coeffs(p, c))) return rc;
   if (!phi0 || !rhs || !phi_out) return set_err(JMG_ERR_VALUE, "phi0, rhs and phi_out must not be NULL");
+  if ((rc = coarse_setup(p))) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   const Box b0 = p->lv[0].box;
   Lvl<double> l0 = lvl64(p, ws, 0);
@@ -599,10 +644,6 @@ int jmg_solve(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs
     launch_distance_snapshot(b0, phi_old, l0.phi, st, s);  // phi_old <- smoothed phi
   }
   // 4. the loop
-  if (p->coarse_smem64 && prepare_coarse_smem<double>(p->dim, p->coarse_smem64))
-    return set_err(JMG_ERR_CUDA, "cannot enable %zu bytes of shared memory for the coarse kernel", p->coarse_smem64);
-  if (p->mixed && p->coarse_smem32 && prepare_coarse_smem<float>(p->dim, p->coarse_smem32))
-    return set_err(JMG_ERR_CUDA, "cannot enable %zu bytes of shared memory for the coarse kernel", p->coarse_smem32);
   const bool runs = p->cfg.max_iters_outer > 0;
   if (runs && !p->host_loop) {
     if ((rc = build_graph(p, ws))) return rc;

@@ -37,12 +37,31 @@ template <typename T> void launch_prolong(int dim, const Lvl<T>& f, const Lvl<T>
 template <typename T>
 void launch_coarse_cycle(int dim, const LvlTable<T>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
                          cudaStream_t s);
-// mg_coarse.cu: the coarse sub-cycle from shared memory (one block)
-size_t coarse_smem_bytes(int dim, const int* m0, int lev0, int last, size_t elem);
-template <typename T> int prepare_coarse_smem(int dim, size_t bytes);
+// mg_coarse.cu: the coarse sub-cycle on one thread-block cluster (rows of every level
+// spread over the CTAs' shared memory)
+constexpr int kMaxClusterRanks = 16;
+struct ClusterLevel {
+  int off;        // element offset of the level's block in every CTA's shared memory
+  int nx, ny;     // padded extents along x and y
+  int rp;         // row pitch in shared memory (nx rounded up to 4 elements)
+  int nrows;      // rows of the level ((my+3) in 2D, (mz+3)(my+3) in 3D)
+  int rpr;        // rows per CTA
+  int dist;       // 1: rows spread over all CTAs; 0: the whole level lives in CTA 0
+  int m[3];
+};
+struct ClusterLayout {
+  int lev0, last, ranks;
+  long long elems;  // elements of shared memory per CTA
+  ClusterLevel l[kMaxLevels];
+};
+// m[l][axis]: resolution of level l. Returns 0 on success.
+int cluster_layout(int dim, const int m[][3], int lev0, int last, int ranks, ClusterLayout* out);
+// sets the kernel's shared-memory / cluster-size attributes and checks that one cluster
+// of `ranks` CTAs fits on the GPU (0: usable)
+template <typename T> int prepare_coarse_cluster(int dim, size_t smem_bytes, int ranks);
 template <typename T>
-void launch_coarse_smem(int dim, const LvlTable<T>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
-                        size_t smem, cudaStream_t s);
+void launch_coarse_cluster(int dim, const LvlTable<T>* tab, const ClusterLayout& lay, const CycleParams& cp,
+                           int fcycle, int skip_pre, size_t smem_bytes, cudaStream_t s);
 // copies a level table into device memory (the coarse kernel reads it from there)
 template <typename T> void launch_store_table(const LvlTable<T>& tab, LvlTable<T>* dst, cudaStream_t s);
 

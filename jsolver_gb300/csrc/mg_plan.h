@@ -29,7 +29,7 @@ struct JmgPlan {
   int dim = 2;
   int levels = 0;       // L of the reference
   int used = 0;         // levels visited: 0..L-2
-  int coarse_start = 0; // first level run by the single-block kernel
+  int coarse_start = 0; // first level run by one coarse sub-cycle kernel
   bool mixed = false;
   std::vector<jmg::LevelInfo> lv;
   size_t off_phi_old = 0, off_state = 0, off_parts = 0, off_tab64 = 0, off_tab32 = 0, ws_bytes = 0;
@@ -44,9 +44,13 @@ struct JmgPlan {
   // after every iteration. Profilers cannot attribute kernel nodes inside graphs that hold
   // conditional nodes; this mode lets them see every launch.
   bool host_loop = false;
-  // shared-memory bytes of the coarse sub-cycle kernel per precision (0: use the
-  // global-memory version, e.g. when the levels do not fit in shared memory)
-  size_t coarse_smem64 = 0, coarse_smem32 = 0;
+  // coarse sub-cycle on a thread-block cluster (cluster_ranks 0: the single-block
+  // global-memory kernel instead, from the first level of at most 8192 points)
+  int cluster_ranks = 0;
+  bool coarse_ready = false;  // coarse_setup done
+  bool force_block = false;   // JMG_COARSE=block at plan creation: no cluster kernel
+  jmg::ClusterLayout cluster{};
+  size_t cluster_smem64 = 0, cluster_smem32 = 0;
 };
 
 
@@ -65,5 +69,7 @@ CycleParams cycle_params(const JmgPlan* p, bool off_diag);
 int check_coeffs(const JmgPlan* p, const JmgCoeffs* c);
 int check_ws(const JmgPlan* p, void* ws, size_t bytes);
 int build_hierarchy(JmgPlan* p, const JmgCoeffs* c, void* ws, cudaStream_t s);
+// chooses the coarse sub-cycle kernel once per plan (needs the GPU; mg_driver.cu)
+int coarse_setup(JmgPlan* p);
 
 }  // namespace jmg

@@ -1,0 +1,135 @@
+"""Learned initial guess: the GPU network (libjmg) against its CPU restatement (oracle/unet.py).
+
+The oracle rounds to BF16 at the same points as the GPU (stored activations and
+activation gradients); the GPU differs in the order of its FP32 sums (tensor-core tiles,
+atomics), which flips an occasional BF16 rounding. Tolerances: forward output 1e-2
+relative L2, loss 1e-3 relative, each layer's weight and bias gradients 3e-2 relative L2.
+"""
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():  # pragma: no cover
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+from jsolver_gb300 import learned as LN  # noqa: E402
+from jsolver_gb300.grid_1d import grid_1D  # noqa: E402
+from jsolver_gb300.solver_2d import solve_2d  # noqa: E402
+from oracle import unet as U  # noqa: E402
+
+DEV = torch.device("cuda", 0)
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-30))
+
+
+def _params(seed):
+    p = U.init_params(seed)
+    rng = np.random.default_rng(seed + 1)
+    for (ws, we), (bs, be) in U.layer_slices():
+        p[bs:be] = rng.standard_normal(be - bs).astype(np.float32) * 0.05
+    # a larger output layer so that the loss gradient is not dominated by rounding
+    (ws, we), _ = U.layer_slices()[-1]
+    p[ws:we] *= 10
+    return p
+
+
+def _inputs(B, res, seed):
+    rng = np.random.default_rng(seed)
+    x = np.zeros((B, res, res, 16), np.float32)
+    x[..., :4] = rng.standard_normal((B, res, res, 4)).astype(np.float32)
+    xb = U.bf(torch.from_numpy(x))
+    return xb, xb.to(torch.bfloat16).to(DEV)
+
+
+def test_param_count():
+    assert LN.num_params() == U.num_params()
+
+
+def test_forward_matches_oracle():
+    res, B = 128, 2
+    p = _params(0)
+    net = LN.GuessNet(res=res, max_batch=B, device=DEV, params=p)
+    xo, xg = _inputs(B, res, 1)
+    y = net.forward(xg).cpu().numpy()
+    yo, _ = U.forward(p, xo)
+    r = rel(y, yo[..., 0].numpy())
+    assert r < 1e-2, r
+
+
+def test_gradients_match_oracle():
+    res, B = 128, 2
+    p = _params(2)
+    net = LN.GuessNet(res=res, max_batch=B, device=DEV, params=p)
+    xo, xg = _inputs(B, res, 3)
+    rng = np.random.default_rng(4)
+    t = rng.standard_normal((B, res, res)).astype(np.float32)
+    loss, g = net.loss_grad(xg, torch.from_numpy(t).to(DEV))
+    lo, go, _ = U.loss_and_grads(p, xo, torch.from_numpy(t))
+    assert abs(float(loss) - lo) <= 1e-3 * abs(lo)
+    g = g.cpu().numpy()
+    for li, ((ws, we), (bs, be)) in enumerate(U.layer_slices()):
+        assert rel(g[ws:we], go[ws:we]) < 3e-2, (li, "W", rel(g[ws:we], go[ws:we]))
+        if np.linalg.norm(go[bs:be]) > 0:
+            assert rel(g[bs:be], go[bs:be]) < 3e-2, (li, "b", rel(g[bs:be], go[bs:be]))
+
+
+def test_train_steps_reduce_loss():
+    res, B = 128, 4
+    net = LN.GuessNet(res=res, max_batch=B, device=DEV, params=LN.init_params(5))
+    _, xg = _inputs(B, res, 6)
+    yy, xx = np.meshgrid(np.linspace(0, 1, res), np.linspace(0, 1, res), indexing="ij")
+    t = torch.from_numpy(np.broadcast_to(np.sin(np.pi * xx) * np.sin(2 * np.pi * yy), (B, res, res))
+                         .astype(np.float32).copy()).to(DEV)
+    l0, _ = net.loss_grad(xg, t)
+    for _ in range(60):
+        net.train_step(xg, t, 2e-3)
+    l1, _ = net.loss_grad(xg, t)
+    assert float(l1) < 0.5 * float(l0), (float(l0), float(l1))
+
+
+@pytest.mark.parametrize("m,res", [(256, 256), (512, 256), (256, 128)])
+def test_inputs_and_guess_mapping(m, res):
+    prob = LN.sample_problems(1, m, 7, DEV)
+    g = grid_1D(m)
+    p = _params(8)
+    net = LN.GuessNet(res=res, max_batch=1, device=DEV, params=p, out_scale=0.02)
+    args = [prob[k][0] for k in ("rhs", "lam", "D_xx", "D_yy")]
+    x, rms = net.inputs(g, g, *args)
+    xo, rmso = U.inputs_2d(m, res, *[a.cpu().numpy() for a in (args[1], args[2], args[3], args[0])])
+    assert abs(float(rms) - rmso) <= 1e-6 * rmso
+    xg = x.float().cpu().numpy()
+    assert np.allclose(xg, xo, rtol=8e-3, atol=1e-6), np.abs(xg - xo).max()
+    phi0 = net.guess(g, g, *args).cpu().numpy()
+    y = net.forward(x[None]).cpu().numpy()[0]
+    ref = U.output_2d(y, rmso, 0.02, m)
+    assert rel(phi0, ref) < 1e-6, rel(phi0, ref)
+
+
+WEIGHTS = LN.WEIGHTS
+
+
+@pytest.mark.skipif(not os.path.exists(WEIGHTS), reason="no trained weights in the package")
+@pytest.mark.parametrize("m", [256, 1024])
+def test_trained_guess_saves_cycles(m):
+    """The committed network against the zero guess on held-out problems of the 2D
+    random-coefficient workload (seeds outside the training range): fewer cycles to the
+    same relative residual 1e-10, which both runs reach."""
+    net = LN.GuessNet.load(WEIGHTS, device=DEV)
+    g = grid_1D(m)
+    zero, learned = [], []
+    for s in range(4):
+        prob = LN.sample_problems(1, m, 10 ** 7 + s, DEV, phi_kind="workload")
+        args = [prob[k][0] for k in ("rhs", "lam", "D_xx", "D_yy")]
+        phi0 = net.guess(g, g, *args)
+        _, c0 = LN.solve_plain(g, prob, 0)
+        _, c1 = LN.solve_plain(g, prob, 0, phi0=phi0)
+        zero.append(int(c0))
+        learned.append(int(c1))
+    assert np.mean(learned) < np.mean(zero), (zero, learned)

@@ -427,3 +427,37 @@ def test_mixed_precision_fixed_and_distance_modes(dim):
     assert rel_l2(phim, ref) < 1e-7
     phif, cf = solve(*gs, *args, precision="mixed", fixed=True, max_iters_outer=cm)
     assert cf == cm and rel_l2(phif, phim) < 1e-12
+
+
+CLUSTER_CASES = [(2, 64, {}), (2, 256, {}), (2, 256, {"gamma": 2}), (2, 256, {"fcycle": True}),
+                 (2, 128, {"skip_pre": True}), (2, 128, {"nu1": 2, "nu2": 0}), (2, 128, {"nu1": 0, "nu2": 2}),
+                 (2, 512, {"precision": "mixed"}), (3, 32, {"fcycle": True}), (3, 64, {}),
+                 (3, 32, {"gamma": 2, "precision": "mixed"})]
+
+
+@pytest.mark.parametrize("dim,m,form", CLUSTER_CASES,
+                         ids=lambda x: ",".join(f"{k}={v}" for k, v in x.items()) if isinstance(x, dict) else str(x))
+def test_cluster_coarse_cycle_matches_single_block(dim, m, form, monkeypatch):
+    """The coarse levels on a thread-block cluster (rows spread over the CTAs' shared
+    memory) against the single-block global-memory kernel (JMG_COARSE=block): the same
+    point arithmetic, so the same phi to rounding and the same cycle count."""
+    g = grid_1D(m)
+    if dim == 2:
+        p = W.random_2d(m, seed=21)
+        grids, fn = (g, g), solve_2d
+        args = (p["phi0"], p["rhs"], p["lam"], p["D_xx"], p["D_yy"])
+    else:
+        p = W.random_3d(m, seed=21)
+        grids, fn = (g, g, g), solve_3d
+        args = (p["phi0"], p["rhs"], p["lam"], p["D_xx"], p["D_yy"], p["D_zz"])
+    kw = dict(form)
+    if kw.get("precision") == "mixed":
+        kw.update(stop="residual", rtol=1e-9)
+    else:
+        kw.update(fixed=True, max_iters_outer=5)
+    phi_c, c_c = fn(*grids, *args, **kw)
+    monkeypatch.setenv("JMG_COARSE", "block")
+    monkeypatch.setattr(_engine, "CACHE", _engine._Cache())
+    phi_b, c_b = fn(*grids, *args, **kw)
+    assert int(c_c) == int(c_b)
+    assert rel_l2(phi_c, phi_b) < 1e-13, rel_l2(phi_c, phi_b)
