@@ -5,6 +5,13 @@ One step = one complete solve (coefficient hierarchy + cycles until
 ``jsolver_gb300.workloads.random_2d(1024, seed)``: D_xx, D_yy = exp(GRF sigma 1, corr.
 length 0.05), lambda ~ U[0, 10], rhs = L_h sin(pi x) sin(2 pi y).
 
+Forms (``--form``): ``fp64`` plain FP64 multigrid from phi0 = 0; ``mixed`` FP32 cycles in
+FP64 iterative refinement; ``learned`` / ``learned-mixed`` the same from the learned
+network's initial guess, whose computation is inside every timed step. The default
+(``auto``) is the headline form: learned-mixed in 2D (when the package holds trained
+weights), mixed in 3D. Every run also times the plain FP64 solve of the same problem
+the same way and reports it under ``plain_fp64``.
+
 Our arm (default): ``value`` is the device time of a solve with inputs resident in HBM,
 through the C ABI (jmg_solve), timed with CUDA events on the solving stream; L2 is
 flushed (256 MB write) before every timed solve. ``e2e`` is the same solve through the
@@ -46,7 +53,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--form", default="auto", choices=["auto", "fp64", "mixed", "learned", "learned-mixed"])
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 comparison solve")
+    ap.add_argument("--inner-cycles", type=int, default=1, help="FP32 cycles per refinement step (mixed forms)")
     ap.add_argument("--workload", default="2d", choices=sorted(WORKLOADS))
     ap.add_argument("--cycle", default=None, choices=["V", "W", "F"])
     ap.add_argument("--m", type=int, default=None)
@@ -58,7 +67,15 @@ def parse():
     a.dim = dim
     a.m = a.m or m
     a.cycle = a.cycle or cyc
+    if a.form == "auto":
+        from jsolver_gb300.learned import WEIGHTS
+        a.form = "learned-mixed" if dim == 2 and os.path.exists(WEIGHTS) else "mixed"
     return a
+
+
+# kernel launches of one learned guess: input pooling, RMS, packing (3); 12 convolutions,
+# 3 poolings, 3 up-adds; the output interpolation (1)
+GUESS_LAUNCHES = 22
 
 
 def make_problem(args, seed):
@@ -170,6 +187,20 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(value, device):
+    """The job's time: the maximum of one float over all ranks (every rank gets it)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seed(seed, rank):
+    """Each replica solves its own seeded problem: no data is exchanged between ranks."""
+    return seed + rank
+
+
 def workload_name(args):
     shape = "^".join([str(args.m + 3), str(args.dim)])
     return f"{args.dim}d-{args.m}^{args.dim}-random-coeff (arrays {shape} float64)"
@@ -216,16 +247,21 @@ def main():
 
     m, dim = args.m, args.dim
     cn = coeff_names(dim)
-    p = make_problem(args, args.seed + rank)
+    p = make_problem(args, replica_seed(args.seed, rank))
     g = grid_1D(m)
     kw = cycle_kw(args.cycle)
-    opts = dict(stop="residual", rtol=RTOL, precision=args.form, max_iters_outer=20000, **kw)
+    learned = args.form.startswith("learned")
+    precision = "mixed" if args.form in ("mixed", "learned-mixed") else "fp64"
+    opts = dict(stop="residual", rtol=RTOL, precision=precision, max_iters_outer=20000, **kw)
+    if precision == "mixed":
+        opts["inner_cycles"] = args.inner_cycles
     lib = _lib.load()
-    cfg = _engine.make_config(**opts)
-    plan = _lib.Plan(_engine.make_grid((g,) * dim), cfg)
+    grid = _engine.make_grid((g,) * dim)
+    plan = _lib.Plan(grid, _engine.make_config(**opts))
     stream = torch.cuda.Stream(dev)
     d = {k: torch.from_numpy(p[k]).to(dev) for k in ["phi0", "rhs", "lam"] + cn}
     out = torch.empty_like(d["phi0"])
+    start = torch.empty_like(d["phi0"])  # the learned guess
     count = torch.zeros((), dtype=torch.int64, device=dev)
     wsb = torch.empty(plan.workspace_bytes, dtype=torch.uint8, device=dev)
     coeffs = _lib.JmgCoeffs()
@@ -234,46 +270,71 @@ def main():
         coeffs.D[k] = d[name].data_ptr()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     vp = ctypes.c_void_p
+    net = None
+    if learned:
+        from jsolver_gb300.learned import GuessNet, WEIGHTS
+        net = GuessNet.load(WEIGHTS, device=dev)
 
-    def solve_dev(s):
-        _lib.check(lib.jmg_solve(plan.handle, vp(d["phi0"].data_ptr()), vp(d["rhs"].data_ptr()), ctypes.byref(coeffs),
-                                 vp(out.data_ptr()), vp(count.data_ptr()), vp(wsb.data_ptr()),
-                                 ctypes.c_size_t(wsb.numel()), vp(s.cuda_stream)))
+    def solve_dev(s, pl=plan, ws=wsb, use_net=learned):
+        phi0 = d["phi0"]
+        if use_net:
+            _lib.check(lib.jmg_net_guess_2d(net.handle, ctypes.byref(grid), ctypes.byref(coeffs),
+                                            vp(d["rhs"].data_ptr()), ctypes.c_float(net.out_scale),
+                                            vp(start.data_ptr()), vp(s.cuda_stream)))
+            phi0 = start
+        _lib.check(lib.jmg_solve(pl.handle, vp(phi0.data_ptr()), vp(d["rhs"].data_ptr()), ctypes.byref(coeffs),
+                                 vp(out.data_ptr()), vp(count.data_ptr()), vp(ws.data_ptr()),
+                                 ctypes.c_size_t(ws.numel()), vp(s.cuda_stream)))
 
-    with torch.cuda.stream(stream):
+    def timed(fn, steps, clocks=None):
         for _ in range(args.warmup):
-            solve_dev(stream)
+            fn(stream)
         stream.synchronize()
-        cycles = int(count.item())
-        # timed region
         if ws_n > 1:
             dist.barrier()
         torch.cuda.synchronize()
         evs = []
-        with Clocks(local) as clk:
-            for _ in range(args.steps):
-                flush.zero_()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                solve_dev(stream)
-                e1.record(stream)
-                evs.append((e0, e1))
-            torch.cuda.synchronize()
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn(stream)
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
         if ws_n > 1:
             dist.barrier()
-        times = [a.elapsed_time(b) for a, b in evs]
-        ms = float(np.mean(times))
-        if ws_n > 1:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        t_ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+        return max_over_ranks(t_ms, dev) if ws_n > 1 else t_ms
+
+    def rel_residual(pl, ws):
+        rr_t = torch.empty((), dtype=torch.float64, device=dev)
+        _lib.check(lib.jmg_rel_residual(pl.handle, vp(out.data_ptr()), vp(d["rhs"].data_ptr()), vp(rr_t.data_ptr()),
+                                        vp(ws.data_ptr()), ctypes.c_size_t(ws.numel()), vp(stream.cuda_stream)))
+        stream.synchronize()
+        return float(rr_t.item())
+
+    with torch.cuda.stream(stream):
+        plain = None
+        if not args.no_compare and args.form != "fp64":
+            # the plain FP64 multigrid from phi0 = 0 on the same problem, timed the same way
+            plan64 = _lib.Plan(grid, _engine.make_config(**dict(opts, precision="fp64", inner_cycles=1)))
+            ws64 = torch.empty(plan64.workspace_bytes, dtype=torch.uint8, device=dev)
+            f64 = lambda s: solve_dev(s, plan64, ws64, False)  # noqa: E731
+            ms64 = timed(f64, args.steps)
+            plain = {"ms": ms64, "cycles": int(count.item()), "final_rel_residual": rel_residual(plan64, ws64)}
+            del ws64
+        with Clocks(local) as clk:
+            ms = timed(solve_dev, args.steps)
         cycles = int(count.item())
         # relative residual of the result, FP64 on the device
-        rr_t = torch.empty((), dtype=torch.float64, device=dev)
-        _lib.check(lib.jmg_rel_residual(plan.handle, vp(out.data_ptr()), vp(d["rhs"].data_ptr()), vp(rr_t.data_ptr()),
-                                        vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()), vp(stream.cuda_stream)))
-        stream.synchronize()
-        rel_res = float(rr_t.item())
+        rel_res = rel_residual(plan, wsb)
+        guess_rel_res = None
+        if learned:
+            solve_dev(stream)  # leaves the guess in `start`
+            out.copy_(start)
+            guess_rel_res = rel_residual(plan, wsb)
+            solve_dev(stream)
         err_exact = (float(np.abs(out.cpu().numpy() - p["phi_exact"]).max()) if "phi_exact" in p else None)
 
         # dominant kernel: the fine-level FP64 red-black sweep (two colour launches), timed
@@ -307,7 +368,9 @@ def main():
             for k in host:
                 dst[k].copy_(host[k], non_blocking=True)
             solve = solve_2d if dim == 2 else solve_3d
-            phi, cnt = solve(*((g,) * dim), dst["phi0"], dst["rhs"], dst["lam"], *[dst[k] for k in cn], **opts)
+            extra = {"guess": net} if learned else {}
+            phi, cnt = solve(*((g,) * dim), dst["phi0"], dst["rhs"], dst["lam"], *[dst[k] for k in cn], **opts,
+                             **extra)
             phi_host.copy_(phi, non_blocking=True)
             cnt_host.copy_(cnt, non_blocking=True)
 
@@ -329,7 +392,7 @@ def main():
 
     fixed_n, per_cycle = ctypes.c_int64(), ctypes.c_int64()
     lib.jmg_plan_launch_counts(plan.handle, ctypes.byref(fixed_n), ctypes.byref(per_cycle))
-    launches = args.steps * (fixed_n.value + per_cycle.value * cycles)
+    launches = args.steps * (fixed_n.value + per_cycle.value * cycles + (GUESS_LAUNCHES if learned else 0))
 
     peaks = {}
     try:
@@ -350,13 +413,18 @@ def main():
         "metric": metric_name(dim, m), "value": ms, "unit": "ms", "n_gpus": ws_n, "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.form == "fp64" else "f32+f64",
+        "dtype": {"fp64": "f64", "mixed": "f32+f64", "learned": "bf16+f64", "learned-mixed": "bf16+f32+f64"}[args.form],
         "data": "synthetic (seeded GRF coefficients, manufactured rhs; no dataset in the reference)",
         "config": {"workload": workload_name(args), "cycle": args.cycle,
-                   "form": args.form, "stop": f"rel. residual <= {RTOL}", "cycles": cycles,
+                   "form": args.form, "stop": f"rel. residual <= {RTOL}",
+                   "cycles": cycles * (args.inner_cycles if precision == "mixed" else 1),
+                   "inner_cycles": args.inner_cycles if precision == "mixed" else None,
                    "l2": "flushed (256 MB write) before every timed solve", "parallelism": f"replicas x{ws_n}"},
         "solves_per_s": 1e3 / ms * ws_n,
         "final_rel_residual": rel_res,
+        "plain_fp64": plain,
+        "speedup_vs_plain_fp64": (plain["ms"] / ms) if plain else None,
+        "guess_rel_residual": guess_rel_res,
         "max_err_vs_exact_discrete": err_exact,
         "roofline": {"bound": "hbm", "kernel": f"k_sweep_color{dim}d<double> (fine level; 2 launches per sweep)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -368,7 +436,9 @@ def main():
     }
     line["clocks"] = clk.summary()
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(p, dim, m, cycles, kw)
+        # the reference's algorithm: plain FP64 cycles from phi0 = 0
+        ref_cycles = plain["cycles"] if plain else cycles
+        line["cpu_baseline"] = cpu_baseline(p, dim, m, ref_cycles, kw)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws_n > 1:

@@ -155,8 +155,12 @@ class Prepared:
         self.coeffs.D_xy = None
 
 
-def solve(grids, phi, rhs, lam, D, D_xy=None, **opts):
-    """Full solve through ``jmg_solve``. ``grids`` is (grid_x, grid_y[, grid_z])."""
+def solve(grids, phi, rhs, lam, D, D_xy=None, guess=None, **opts):
+    """Full solve through ``jmg_solve``. ``grids`` is (grid_x, grid_y[, grid_z]).
+
+    ``guess``: None starts from ``phi`` (the reference); ``"learned"`` (the package's
+    trained network) or a ``learned.GuessNet`` replaces phi's values by the network's
+    prediction (2D square grids; phi still fixes the shape and dtype rules)."""
     ndim = len(grids)
     cfg = make_config(**opts)
     grid = make_grid(grids)
@@ -167,6 +171,8 @@ def solve(grids, phi, rhs, lam, D, D_xy=None, **opts):
     torch_in = any(is_cuda_tensor(a) for a in [phi, rhs, lam] + list(D))
     wants_grad = torch.is_grad_enabled() and any(isinstance(a, torch.Tensor) and a.requires_grad
                                                  for a in [phi, rhs, lam] + list(D))
+    if guess is not None and (ndim != 2 or wants_grad):
+        raise ValueError("guess= is available for 2D solves without gradients")
     if wants_grad:
         if not cfg.fixed:
             raise ValueError("reverse-mode differentiation needs fixed=True, as in the reference "
@@ -180,6 +186,9 @@ def solve(grids, phi, rhs, lam, D, D_xy=None, **opts):
     with torch.cuda.device(device):
         phi_d = to_device(phi, device)
         rhs_d = to_device(rhs, device)
+        if guess is not None:
+            from .learned import predict_phi0
+            phi_d = predict_phi0(guess, grids, rhs_d, lam, D, device)
         prep = Prepared(ndim, device, lam, D, D_xy, sl, spatial)
         out = torch.empty_like(phi_d)
         count = torch.empty((), dtype=torch.int64, device=device)

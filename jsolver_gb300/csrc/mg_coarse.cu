@@ -19,6 +19,8 @@
 // the reference's order, so results are bit-identical to them.
 #include <cooperative_groups.h>
 
+#include <type_traits>
+
 #include "mg_common.cuh"
 #include "mg_kernels.h"
 
@@ -71,7 +73,7 @@ struct DLevel {
   }
   // array-0 (phi) pointer of row s, wherever it lives; array a is at + a * as
   __device__ __forceinline__ T* rowp(const Ctx<T>& c, int s) const {
-    if (!dist) return c.sm + off + s * rp;
+    if (!dist) return (c.me == 0 ? c.sm : c.rb[0]) + off + s * rp;  // the level lives in CTA 0
     if (s >= s0 && s < s0 + rpr) return c.sm + off + (s - s0) * rp;
     const int r = s / rpr;
     return c.rb[r] + off + (s - r * rpr) * rp;
@@ -278,10 +280,6 @@ __device__ void p_prolong(const Ctx<T>& c, const DLevel<T, DIM>& f, const DLevel
   }
 }
 
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)),
-               "l"(gmem));
-}
 
 template <typename T, int DIM>
 __global__ void __launch_bounds__(kThreads) k_coarse_cluster(const LvlTable<T>* __restrict__ tab, ClusterLayout lay,
@@ -296,30 +294,45 @@ __global__ void __launch_bounds__(kThreads) k_coarse_cluster(const LvlTable<T>* 
   if (threadIdx.x < lay.ranks) rb[threadIdx.x] = cluster.map_shared_rank(c.sm, (int)threadIdx.x);
   const int lev0 = lay.lev0;
 
-  // stage the owned rows in shared memory with 16-byte asynchronous copies: the
-  // coefficients of every level, phi and rhs of the entry level. A global row starts on
-  // a 128-byte boundary and its pitch covers the copied rp >= nx elements.
-  constexpr int kV = 16 / sizeof(T);  // elements per copy
+  // stage the owned rows in shared memory: the coefficients of every level, phi and rhs
+  // of the entry level, in 16-byte loads through L2, four in flight per thread. A global
+  // row starts on a 64-byte boundary and its pitch covers the copied rp >= nx elements.
+  using V = typename std::conditional<sizeof(T) == 8, double2, float4>::type;
+  constexpr int kV = 16 / sizeof(T);  // elements per load
   for (int l = lev0; l <= lay.last; ++l) {
     DLevel<T, DIM> v;
     v.init(lay.l[l - lev0], c.me);
     const Lvl<T>& g = tab->l[l];
-    const int cpr = v.rp / kV;  // copies per row
+    const int cpr = v.rp / kV;  // loads per row
     const int n = (v.s1 - v.s0) * cpr;
     const int na = DIM == 3 ? 7 : 6;
     for (int a = l == lev0 ? A_PHI : A_WX; a < na; ++a) {
       const T* src = a == A_PHI ? g.phi : a == A_RHS ? g.rhs : a == A_WX ? g.wx : a == A_WY ? g.wy
                    : a == A_ACC ? g.acc : a == A_INVD ? g.invd : g.wz;
       T* dst = c.sm + v.off + a * v.as;
-      for (int t = threadIdx.x; t < n; t += kThreads) {
-        const int q = t / cpr, e = (t - q * cpr) * kV;
-        const int s = v.s0 + q;
-        const int k = DIM == 3 ? s / v.ny : 0, j = s - k * v.ny;
-        cp_async16(dst + q * v.rp + e, src + (long long)k * g.S + (long long)j * g.P + e);
+      for (int t0 = threadIdx.x; t0 < n; t0 += 4 * kThreads) {
+        V buf[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int t = t0 + u * kThreads;
+          if (t < n) {
+            const int q = t / cpr, e = (t - q * cpr) * kV;
+            const int s = v.s0 + q;
+            const int k = DIM == 3 ? s / v.ny : 0, j = s - k * v.ny;
+            buf[u] = __ldcg(reinterpret_cast<const V*>(src + (long long)k * g.S + (long long)j * g.P + e));
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int t = t0 + u * kThreads;
+          if (t < n) {
+            const int q = t / cpr, e = (t - q * cpr) * kV;
+            *reinterpret_cast<V*>(dst + q * v.rp + e) = buf[u];
+          }
+        }
       }
     }
   }
-  asm volatile("cp.async.wait_all;\n" ::: "memory");
   cluster.sync();
 
   // pass bookkeeping: a pass on a spread level, or one following a CTA-0-only pass that

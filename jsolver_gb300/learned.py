@@ -159,6 +159,29 @@ class GuessNet:
         return phi0
 
 
+_DEFAULT = {}
+
+
+def default_net(device):
+    """The package's trained network on `device` (loaded once per device)."""
+    key = str(device)
+    if key not in _DEFAULT:
+        if not os.path.exists(WEIGHTS):
+            raise FileNotFoundError(f"no trained weights at {WEIGHTS}: train them with "
+                                    "`python -m jsolver_gb300.learned train`")
+        _DEFAULT[key] = GuessNet.load(WEIGHTS, device=device)
+    return _DEFAULT[key]
+
+
+def predict_phi0(guess, grids, rhs, lam, D, device):
+    """phi0 from the network ('learned' = the package's weights, or a GuessNet)."""
+    net = default_net(device) if isinstance(guess, str) and guess == "learned" else guess
+    if not isinstance(net, GuessNet):
+        raise ValueError("guess must be None, 'learned' or a GuessNet")
+    gx, gy = grids
+    return net.guess(gx, gy, rhs, lam, D[0], D[1])
+
+
 # ---- problem sampling (torch on the GPU; the distributions of workloads.random_2d) ------
 
 def _grf(n, shape, h, corr_len, sigma, gen, device):

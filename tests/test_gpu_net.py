@@ -88,7 +88,7 @@ def test_train_steps_reduce_loss():
     t = torch.from_numpy(np.broadcast_to(np.sin(np.pi * xx) * np.sin(2 * np.pi * yy), (B, res, res))
                          .astype(np.float32).copy()).to(DEV)
     l0, _ = net.loss_grad(xg, t)
-    for _ in range(60):
+    for _ in range(200):
         net.train_step(xg, t, 2e-3)
     l1, _ = net.loss_grad(xg, t)
     assert float(l1) < 0.5 * float(l0), (float(l0), float(l1))
