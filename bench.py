@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--form", default="auto", choices=["auto", "fp64", "mixed", "learned", "learned-mixed"])
     ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 comparison solve")
     ap.add_argument("--inner-cycles", type=int, default=1, help="FP32 cycles per refinement step (mixed forms)")
+    ap.add_argument("--outer", default="richardson", choices=["richardson", "fcg"],
+                    help="iterate the cycle (reference) or use it as the preconditioner of flexible CG")
     ap.add_argument("--workload", default="2d", choices=sorted(WORKLOADS))
     ap.add_argument("--cycle", default=None, choices=["V", "W", "F"])
     ap.add_argument("--m", type=int, default=None)
@@ -252,7 +254,7 @@ def main():
     kw = cycle_kw(args.cycle)
     learned = args.form.startswith("learned")
     precision = "mixed" if args.form in ("mixed", "learned-mixed") else "fp64"
-    opts = dict(stop="residual", rtol=RTOL, precision=precision, max_iters_outer=20000, **kw)
+    opts = dict(stop="residual", rtol=RTOL, precision=precision, max_iters_outer=20000, outer=args.outer, **kw)
     if precision == "mixed":
         opts["inner_cycles"] = args.inner_cycles
     lib = _lib.load()
@@ -316,9 +318,10 @@ def main():
 
     with torch.cuda.stream(stream):
         plain = None
-        if not args.no_compare and args.form != "fp64":
+        if not args.no_compare and (args.form != "fp64" or args.outer != "richardson"):
             # the plain FP64 multigrid from phi0 = 0 on the same problem, timed the same way
-            plan64 = _lib.Plan(grid, _engine.make_config(**dict(opts, precision="fp64", inner_cycles=1)))
+            plan64 = _lib.Plan(grid, _engine.make_config(**dict(opts, precision="fp64", inner_cycles=1,
+                                                                outer="richardson")))
             ws64 = torch.empty(plan64.workspace_bytes, dtype=torch.uint8, device=dev)
             f64 = lambda s: solve_dev(s, plan64, ws64, False)  # noqa: E731
             ms64 = timed(f64, args.steps)
@@ -418,7 +421,7 @@ def main():
         "config": {"workload": workload_name(args), "cycle": args.cycle,
                    "form": args.form, "stop": f"rel. residual <= {RTOL}",
                    "cycles": cycles * (args.inner_cycles if precision == "mixed" else 1),
-                   "inner_cycles": args.inner_cycles if precision == "mixed" else None,
+                   "inner_cycles": args.inner_cycles if precision == "mixed" else None, "outer": args.outer,
                    "l2": "flushed (256 MB write) before every timed solve", "parallelism": f"replicas x{ws_n}"},
         "solves_per_s": 1e3 / ms * ws_n,
         "final_rel_residual": rel_res,

@@ -48,6 +48,7 @@ enum {
 
 enum { JMG_STOP_DISTANCE = 0, JMG_STOP_RESIDUAL = 1 };
 enum { JMG_PREC_FP64 = 0, JMG_PREC_MIXED = 1 };
+enum { JMG_OUTER_RICHARDSON = 0, JMG_OUTER_FCG = 1 };
 
 /* Geometry: the fields of grid_1D the solver reads (jsolver/grid_1d.py:82-114). */
 typedef struct JmgGrid {
@@ -72,6 +73,9 @@ typedef struct JmgConfig {
   double rtol;             /* relative-residual target for JMG_STOP_RESIDUAL */
   int32_t precision;       /* JMG_PREC_FP64 or JMG_PREC_MIXED (FP32 cycles, FP64 refinement) */
   int32_t inner_cycles;    /* FP32 cycles per refinement step (JMG_PREC_MIXED) */
+  int32_t outer;           /* JMG_OUTER_RICHARDSON (reference: phi += cycle correction) or
+                              JMG_OUTER_FCG (the cycle preconditions flexible CG; needs
+                              JMG_STOP_RESIDUAL or fixed; no reference counterpart) */
 } JmgConfig;
 
 /* Coefficients of one solve: lam, D_xx, D_yy (, D_zz) and optional D_xy. */

@@ -24,11 +24,12 @@ INT32_MAX = int(np.iinfo(np.int32).max)
 
 _PREC = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
 _STOP = {"distance": _lib.STOP_DISTANCE, "residual": _lib.STOP_RESIDUAL}
+_OUTER = {"richardson": _lib.OUTER_RICHARDSON, "fcg": _lib.OUTER_FCG}
 
 
 def make_config(fixed=False, epsilon=1e-12, gamma=1, fcycle=False, skip_pre=False, nu1=1, nu2=1,
                 max_iters_outer=INT32_MAX, max_iters_inner=INT32_MAX, stop="distance", rtol=1e-10,
-                precision="fp64", inner_cycles=1):
+                precision="fp64", inner_cycles=1, outer="richardson"):
     c = _lib.default_config()
     c.fixed = int(bool(fixed))
     c.epsilon = float(epsilon)
@@ -47,6 +48,9 @@ def make_config(fixed=False, epsilon=1e-12, gamma=1, fcycle=False, skip_pre=Fals
     c.rtol = float(rtol)
     c.precision = _PREC[precision]
     c.inner_cycles = int(inner_cycles)
+    if outer not in _OUTER:
+        raise ValueError(f"outer must be one of {sorted(_OUTER)}, got {outer!r}")
+    c.outer = _OUTER[outer]
     return c
 
 

@@ -13,6 +13,7 @@ LIB_PATH = os.path.join(HERE, "libjmg.so")
 JMG_OK, JMG_ERR_VALUE, JMG_ERR_CUDA, JMG_ERR_WORKSPACE = 0, 1, 2, 3
 STOP_DISTANCE, STOP_RESIDUAL = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
+OUTER_RICHARDSON, OUTER_FCG = 0, 1
 
 
 class JmgGrid(ctypes.Structure):
@@ -25,7 +26,7 @@ class JmgConfig(ctypes.Structure):
                 ("skip_pre", ctypes.c_int32), ("nu1", ctypes.c_int32), ("nu2", ctypes.c_int32),
                 ("max_iters_outer", ctypes.c_int64), ("max_iters_inner", ctypes.c_int64),
                 ("epsilon", ctypes.c_double), ("stop", ctypes.c_int32), ("rtol", ctypes.c_double),
-                ("precision", ctypes.c_int32), ("inner_cycles", ctypes.c_int32)]
+                ("precision", ctypes.c_int32), ("inner_cycles", ctypes.c_int32), ("outer", ctypes.c_int32)]
 
 
 class JmgCoeffs(ctypes.Structure):

@@ -60,6 +60,11 @@ int block_coarse_start(const JmgPlan* p) {
 
 int validate_and_layout(JmgPlan* p) {
   const JmgGrid& g = p->grid;
+  if (p->cfg.outer != JMG_OUTER_RICHARDSON && p->cfg.outer != JMG_OUTER_FCG)
+    return set_err(JMG_ERR_VALUE, "outer must be JMG_OUTER_RICHARDSON or JMG_OUTER_FCG, got %d", p->cfg.outer);
+  if (p->cfg.outer == JMG_OUTER_FCG && !p->cfg.fixed && p->cfg.stop != JMG_STOP_RESIDUAL)
+    return set_err(JMG_ERR_VALUE, "outer='fcg' needs stop='residual' or fixed=True (the distance test "
+                                  "measures a stationary iteration)");
   if (g.ndim != 2 && g.ndim != 3) return set_err(JMG_ERR_VALUE, "ndim must be 2 or 3, got %d", g.ndim);
   const char* names[3] = {"x", "y", "z"};
   const int d = g.ndim;
@@ -139,13 +144,25 @@ int validate_and_layout(JmgPlan* p) {
   }
   p->off_tab64 = take(sizeof(LvlTable<double>));
   p->off_tab32 = take(sizeof(LvlTable<float>));
+  p->fcg = p->cfg.outer == JMG_OUTER_FCG;
+  if (p->fcg) {
+    const size_t b8 = p->lv[0].elems * 8;
+    p->off_rho = take(b8);
+    p->off_d = take(b8);
+    p->off_q = take(b8);
+    p->off_z64 = p->mixed ? 0 : take(b8);
+    p->off_fcg_parts = take((size_t)fcg_num_parts() * 5 * 8);
+    p->off_tab64z = take(sizeof(LvlTable<double>));
+  }
   p->ws_bytes = off;
   // the coarse levels are chosen at the first solve (coarse_setup), when the GPU's
   // cluster support is known; until then the single-block rule holds
   p->coarse_start = block_coarse_start(p);
   {
+    // JMG_COARSE=cluster selects the thread-block-cluster coarse kernel; the default is
+    // the single-block kernel, measured as fast or faster at every size on GB300
     const char* cm = getenv("JMG_COARSE");
-    p->force_block = cm && std::strcmp(cm, "block") == 0;
+    p->force_block = !(cm && std::strcmp(cm, "cluster") == 0);
   }
   const char* hl = getenv("JMG_HOST_LOOP");
   p->host_loop = hl && hl[0] == '1';
@@ -154,10 +171,13 @@ int validate_and_layout(JmgPlan* p) {
 
 
 }  // namespace
-// How the coarse levels of a cycle run. A thread-block cluster of 16 CTAs (8 where 16
-// is not allowed) takes every level from the first one of at most 20 000 padded points
-// whose rows, with the levels below, fit in 200 KB of shared memory per CTA; without
-// cluster support one block runs the levels of at most 8192 points from global memory.
+// How the coarse levels of a cycle run. By default one block runs the levels of at most
+// 8192 points from global memory. With JMG_COARSE=cluster (and cluster support) a
+// thread-block cluster of 16 CTAs (8 where 16 is not allowed) takes every level from
+// the first one of at most 20 000 padded points whose rows, with the levels below, fit
+// in 200 KB of shared memory per CTA. On GB300 the coarse levels are bound by the
+// latency of short FP64 dependency chains, not by one SM's FP64 rate, so the cluster
+// gains nothing (measured per cycle: 2D 1024^2 180 us cluster vs 176 us block).
 int jmg::coarse_setup(JmgPlan* p) {
   if (p->coarse_ready) return JMG_OK;
   const int last = p->used - 1;
@@ -314,19 +334,61 @@ void emit_cycle(const JmgPlan* p, LvlTable<T>& tab, const LvlTable<T>* dtab, con
 // starts with a sweep at level 0 from a zero guess (no zeroing pass), and one tiled FP64
 // kernel gives both the stopping test's residual and the next step's FP32 right-hand side.
 bool mixed_fused(const JmgPlan* p) {
-  return p->mixed && p->dim == 2 && p->cfg.stop == JMG_STOP_RESIDUAL && !p->cfg.fixed && p->coarse_start > 0 &&
+  return !p->fcg && p->mixed && p->dim == 2 && p->cfg.stop == JMG_STOP_RESIDUAL && !p->cfg.fixed && p->coarse_start > 0 &&
          p->cfg.nu1 >= 1 && p->cfg.nu2 >= 1;
 }
 
 // Mixed precision with the residual stop in any other case (3D, small grids, nu = 0):
 // one FP64 pass computes the residual norm and the FP32 right-hand side together.
 bool mixed_resid(const JmgPlan* p) {
-  return p->mixed && !mixed_fused(p) && p->cfg.stop == JMG_STOP_RESIDUAL && !p->cfg.fixed;
+  return !p->fcg && p->mixed && !mixed_fused(p) && p->cfg.stop == JMG_STOP_RESIDUAL && !p->cfg.fixed;
 }
 
 int loop_mode(const JmgPlan* p) {
   if (p->cfg.fixed) return 2;
   return p->cfg.stop == JMG_STOP_RESIDUAL ? 1 : 0;
+}
+
+// FCG step: z = cycle(rho) from z = 0 (FP32 inside refinement, or FP64), then the FCG
+// update (mg_krylov.cu) and the loop test on ||rho||.
+void emit_fcg_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaStream_t s) {
+  LoopState* st = ptr<LoopState>(ws, p->off_state);
+  Lvl<double> l0 = lvl64(p, ws, 0);
+  CycleParams cp = cycle_params(p, false);
+  double* fp = ptr<double>(ws, p->off_fcg_parts);
+  const int np = fcg_num_parts();
+  double* rho = ptr<double>(ws, p->off_rho);
+  double* d = ptr<double>(ws, p->off_d);
+  double* q = ptr<double>(ws, p->off_q);
+  const int inner = p->cfg.inner_cycles > 0 ? p->cfg.inner_cycles : 1;
+  // the first sweep may start from a zero guess without reading phi when level 0 runs its
+  // own sweeps; otherwise the correction is zeroed first
+  const bool zero_first = p->coarse_start > 0 && p->cfg.nu1 >= 1;
+  if (p->mixed) {
+    LvlTable<float> t32 = make_table<float>(p, ws);
+    if (!zero_first) cudaMemsetAsync(t32.l[0].phi, 0, p->lv[0].elems * 4, s);
+    for (int k = 0; k < inner; ++k) {
+      EmitTop top;
+      top.zero_first = zero_first && k == 0;
+      emit_cycle<float>(p, t32, ptr<LvlTable<float>>(ws, p->off_tab32), cp, 0, p->cfg.fcycle != 0, false, s,
+                        nullptr, &top);
+    }
+    launch_fcg_iter<float>(p->dim, l0, t32.l[0].phi, d, q, rho, t32.l[0].rhs, fp, fp + 2 * np, fp + 4 * np, s);
+  } else {
+    LvlTable<double> tz = make_table<double>(p, ws);
+    tz.l[0].phi = ptr<double>(ws, p->off_z64);
+    tz.l[0].rhs = rho;
+    if (!zero_first) cudaMemsetAsync(tz.l[0].phi, 0, p->lv[0].elems * 8, s);
+    for (int k = 0; k < inner; ++k) {
+      EmitTop top;
+      top.zero_first = zero_first && k == 0;
+      emit_cycle<double>(p, tz, ptr<LvlTable<double>>(ws, p->off_tab64z), cp, 0, p->cfg.fcycle != 0, false, s,
+                         nullptr, &top);
+    }
+    launch_fcg_iter<double>(p->dim, l0, tz.l[0].phi, d, q, rho, nullptr, fp, fp + 2 * np, fp + 4 * np, s);
+  }
+  launch_loop_step(st, fp + 4 * np, np, loop_mode(p), p->cfg.epsilon, p->cfg.rtol, p->cfg.max_iters_outer, handle,
+                   s);
 }
 
 // body of one loop iteration (captured into the WHILE node's body graph)
@@ -337,6 +399,10 @@ void emit_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaStream
   Lvl<double> l0 = lvl64(p, ws, 0);
   CycleParams cp = cycle_params(p, false);
   int nparts = p->nparts;
+  if (p->fcg) {
+    emit_fcg_body(p, ws, handle, s);
+    return;
+  }
   if (!p->mixed) {
     LvlTable<double> tab = make_table<double>(p, ws);
     emit_cycle<double>(p, tab, ptr<LvlTable<double>>(ws, p->off_tab64), cp, 0, p->cfg.fcycle != 0,
@@ -382,6 +448,13 @@ void emit_prologue(const JmgPlan* p, void* ws, unsigned long long handle, cudaSt
   double* parts = ptr<double>(ws, p->off_parts);
   Lvl<double> l0 = lvl64(p, ws, 0);
   int nparts = p->nparts;
+  if (p->fcg) {
+    double* fp = ptr<double>(ws, p->off_fcg_parts);
+    launch_fcg_init(p->dim, l0, ptr<double>(ws, p->off_rho), ptr<double>(ws, p->off_d), ptr<double>(ws, p->off_q),
+                    p->mixed ? lvl32(p, ws, 0).rhs : nullptr, fp, s);
+    launch_loop_init(st, fp, fcg_num_parts(), mode, p->cfg.rtol, p->cfg.max_iters_outer, handle, s);
+    return;
+  }
   if (mixed_fused(p)) {
     launch_residual_f32_2d(l0, lvl32(p, ws, 0).rhs, parts, s);
     nparts = residual_f32_parts2d(l0.mx, l0.my);
@@ -396,6 +469,20 @@ void emit_prologue(const JmgPlan* p, void* ws, unsigned long long handle, cudaSt
 long long body_launches(const JmgPlan* p) {
   long long n = 0;
   CycleParams cp = cycle_params(p, false);
+  if (p->fcg) {
+    const int inner = p->cfg.inner_cycles > 0 ? p->cfg.inner_cycles : 1;
+    const bool zero_first = p->coarse_start > 0 && p->cfg.nu1 >= 1;
+    if (p->mixed) {
+      LvlTable<float> t;
+      memset(&t, 0, sizeof(t));
+      for (int k = 0; k < inner; ++k) emit_cycle<float>(p, t, nullptr, cp, 0, p->cfg.fcycle != 0, false, nullptr, &n);
+    } else {
+      LvlTable<double> t;
+      memset(&t, 0, sizeof(t));
+      for (int k = 0; k < inner; ++k) emit_cycle<double>(p, t, nullptr, cp, 0, p->cfg.fcycle != 0, false, nullptr, &n);
+    }
+    return n + 3 + 1 + (zero_first ? 0 : 1);  // FCG update, loop step (+ memset node)
+  }
   if (!p->mixed) {
     LvlTable<double> t;
     memset(&t, 0, sizeof(t));
@@ -568,6 +655,7 @@ void jmg_config_default(JmgConfig* c) {
   c->rtol = 1e-10;
   c->precision = JMG_PREC_FP64;
   c->inner_cycles = 1;
+  c->outer = JMG_OUTER_RICHARDSON;
 }
 
 int jmg_plan_create(JmgPlan** out, const JmgGrid* grid, const JmgConfig* cfg) {
@@ -625,6 +713,20 @@ int jmg_solve(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs
   // 2. coefficients, and the level tables the single-block coarse kernel reads
   if ((rc = build_hierarchy(p, c, ws, s))) return rc;
   launch_store_table<double>(make_table<double>(p, ws), ptr<LvlTable<double>>(ws, p->off_tab64), s);
+  if (p->fcg) {
+    // zero frames of the FCG vectors (their kernels write interiors only)
+    const size_t b8 = p->lv[0].elems * 8;
+    JMG_CUDA(cudaMemsetAsync(ptr<char>(ws, p->off_rho), 0, b8, s));
+    JMG_CUDA(cudaMemsetAsync(ptr<char>(ws, p->off_d), 0, b8, s));
+    JMG_CUDA(cudaMemsetAsync(ptr<char>(ws, p->off_q), 0, b8, s));
+    if (!p->mixed) {
+      JMG_CUDA(cudaMemsetAsync(ptr<char>(ws, p->off_z64), 0, b8, s));
+      LvlTable<double> tz = make_table<double>(p, ws);
+      tz.l[0].phi = ptr<double>(ws, p->off_z64);
+      tz.l[0].rhs = ptr<double>(ws, p->off_rho);
+      launch_store_table<double>(tz, ptr<LvlTable<double>>(ws, p->off_tab64z), s);
+    }
+  }
   if (p->mixed) {
     launch_store_table<float>(make_table<float>(p, ws), ptr<LvlTable<float>>(ws, p->off_tab32), s);
     // zero frames of the FP32 correction and residual of level 0 (kernels write only interiors)

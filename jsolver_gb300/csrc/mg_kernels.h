@@ -100,6 +100,16 @@ void launch_add_correction(int dim, const Lvl<double>& a, const float* e32, cuda
 void launch_zero_f32(const Box& b, float* x, cudaStream_t s);
 void launch_convert_f32(const Box& b, const double* src, float* dst, cudaStream_t s);
 
+// mg_krylov.cu: FCG(1) around the cycle (outer = FCG)
+int fcg_num_parts();
+// rho = rhs - L x (x = a.phi), d = q = 0, r32 = float(rho) (nullable); partials of rho^2
+void launch_fcg_init(int dim, const Lvl<double>& a, double* rho, double* d, double* q, float* r32, double* parts,
+                     cudaStream_t s);
+// one FCG step after the preconditioner produced z: dots, direction, update (3 launches)
+template <typename TZ>
+void launch_fcg_iter(int dim, const Lvl<double>& a, const TZ* z, double* d, double* q, double* rho, float* r32,
+                     double* parts_dots, double* parts_dir, double* parts_res, cudaStream_t s);
+
 // mg_driver.cu: records the message jmg_last_error() returns; returns code
 int set_error_message(int code, const char* msg);
 

@@ -1,0 +1,221 @@
+// mg_krylov.cu — flexible conjugate gradients around the multigrid cycle (outer = FCG).
+//
+// The reference iterates the cycle as a stationary method: phi <- phi + M(rhs - L phi).
+// With JmgConfig.outer = JMG_OUTER_FCG the same cycle M (FP64, or FP32 inside FP64
+// refinement) preconditions FCG(1), the flexible CG of Notay (SIAM J. Sci. Comput. 22,
+// 2000) truncated to one previous direction, which tolerates a preconditioner that is
+// neither symmetric nor fixed (a red-black V-cycle, FP32 rounding). With A = -L (SPD for
+// D > 0, lambda >= 0) and rho = rhs - L x:
+//   z = M(rho);  beta = (z . q) / (d . q);  d <- z - beta d;  q <- L z - beta q  (= L d)
+//   alpha = (d . rho) / (d . q);  x <- x + alpha d;  rho <- rho - alpha q
+// All vectors and dot products are FP64; the dot products are reduced in a fixed order
+// (kBlocks per-block partials, summed by every consumer block in the same order), so a
+// solve is bitwise reproducible. The stopping test reads ||rho||, the recurrence
+// residual; it tracks the true residual to FP64 rounding over the few dozen steps a solve
+// takes (checked against jmg_rel_residual in the tests).
+#include "mg_common.cuh"
+#include "mg_kernels.h"
+
+namespace jmg {
+
+namespace {
+
+constexpr int kBlocks = 304;  // fixed, so the reduction order is fixed
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// sums of two values over the block; valid in thread 0
+__device__ __forceinline__ void block_sum2(double& a, double& b) {
+  __shared__ double sa[32], sb[32];
+  a = warp_sum(a);
+  b = warp_sum(b);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    sa[wid] = a;
+    sb[wid] = b;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    a = lane < (int)(blockDim.x >> 5) ? sa[lane] : 0.0;
+    b = lane < (int)(blockDim.x >> 5) ? sb[lane] : 0.0;
+    a = warp_sum(a);
+    b = warp_sum(b);
+  }
+}
+
+// the two totals of a [kBlocks][2] partial array, in a fixed order, in every thread
+__device__ __forceinline__ void totals2(const double* parts, double* t0, double* t1) {
+  __shared__ double s[2];
+  if (threadIdx.x < 32) {
+    double a = 0.0, b = 0.0;
+    for (int t = threadIdx.x; t < kBlocks; t += 32) {
+      a += parts[2 * t];
+      b += parts[2 * t + 1];
+    }
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if (threadIdx.x == 0) {
+      s[0] = a;
+      s[1] = b;
+    }
+  }
+  __syncthreads();
+  *t0 = s[0];
+  *t1 = s[1];
+}
+
+template <int DIM>
+__device__ __forceinline__ bool point(const Lvl<double>& a, long long t, long long* p) {
+  const int nx = a.mx - 1, ny = a.my - 1, nz = DIM == 3 ? a.mz - 1 : 1;
+  if (t >= (long long)nx * ny * nz) return false;
+  const int i = 2 + (int)(t % nx);
+  const int j = 2 + (int)((t / nx) % ny);
+  const int k = 2 + (int)(t / ((long long)nx * ny));
+  *p = DIM == 2 ? (long long)j * a.P + i : (long long)k * a.S + (long long)j * a.P + i;
+  return true;
+}
+
+template <int DIM>
+__device__ __forceinline__ long long npoints(const Lvl<double>& a) {
+  return (long long)(a.mx - 1) * (a.my - 1) * (DIM == 3 ? a.mz - 1 : 1);
+}
+
+// L z at p (FP64 arithmetic on z's values): -(A_cc z - sum of couplings * neighbours),
+// in the order of the defect (mg_common.cuh: defect_point2d/3d)
+template <int DIM, typename TZ>
+__device__ __forceinline__ double apply_L(const Lvl<double>& a, const TZ* z, long long p) {
+  double t = a.acc[p] * (double)z[p];
+  t = fma(-a.wx[p - 1], (double)z[p - 1], t);
+  t = fma(-a.wx[p], (double)z[p + 1], t);
+  t = fma(-a.wy[p - a.P], (double)z[p - a.P], t);
+  t = fma(-a.wy[p], (double)z[p + a.P], t);
+  if (DIM == 3) {
+    t = fma(-a.wz[p - a.S], (double)z[p - a.S], t);
+    t = fma(-a.wz[p], (double)z[p + a.S], t);
+  }
+  return -t;
+}
+
+// rho = rhs - L x, d = q = 0, r32 = float(rho); partials of rho . rho
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) k_fcg_init(Lvl<double> a, double* rho, double* d, double* q, float* r32,
+                                                      double* parts) {
+  double s = 0.0, unused = 0.0;
+  const long long n = npoints<DIM>(a);
+  for (long long t = blockIdx.x * (long long)kThreads + threadIdx.x; t < n; t += (long long)kBlocks * kThreads) {
+    long long p;
+    point<DIM>(a, t, &p);
+    const double r = DIM == 2 ? defect_point2d<double>(a.phi, a.rhs, a.wx, a.wy, a.acc, p, a.P)
+                              : defect_point3d<double>(a.phi, a.rhs, a.wx, a.wy, a.wz, a.acc, p, a.P, a.S);
+    rho[p] = r;
+    d[p] = 0.0;
+    q[p] = 0.0;
+    if (r32) r32[p] = (float)r;
+    s = fma(r, r, s);
+  }
+  block_sum2(s, unused);
+  if (threadIdx.x == 0) parts[blockIdx.x] = s;
+}
+
+// partials of z . q and d . q (the previous direction)
+template <int DIM, typename TZ>
+__global__ void __launch_bounds__(kThreads) k_fcg_dots(Lvl<double> a, const TZ* z, const double* d, const double* q,
+                                                      double* parts) {
+  double zq = 0.0, dq = 0.0;
+  const long long n = npoints<DIM>(a);
+  for (long long t = blockIdx.x * (long long)kThreads + threadIdx.x; t < n; t += (long long)kBlocks * kThreads) {
+    long long p;
+    point<DIM>(a, t, &p);
+    const double qp = q[p];
+    zq = fma((double)z[p], qp, zq);
+    dq = fma(d[p], qp, dq);
+  }
+  block_sum2(zq, dq);
+  if (threadIdx.x == 0) {
+    parts[2 * blockIdx.x] = zq;
+    parts[2 * blockIdx.x + 1] = dq;
+  }
+}
+
+// beta from the dots; d <- z - beta d, q <- L z - beta q; partials of d . rho and d . q
+template <int DIM, typename TZ>
+__global__ void __launch_bounds__(kThreads) k_fcg_dir(Lvl<double> a, const TZ* z, double* d, double* q,
+                                                     const double* rho, const double* parts_in, double* parts) {
+  double zq, dq;
+  totals2(parts_in, &zq, &dq);
+  const double beta = dq != 0.0 ? zq / dq : 0.0;
+  double dr = 0.0, dqn = 0.0;
+  const long long n = npoints<DIM>(a);
+  for (long long t = blockIdx.x * (long long)kThreads + threadIdx.x; t < n; t += (long long)kBlocks * kThreads) {
+    long long p;
+    point<DIM>(a, t, &p);
+    const double dn = fma(-beta, d[p], (double)z[p]);
+    const double qn = fma(-beta, q[p], apply_L<DIM, TZ>(a, z, p));
+    d[p] = dn;
+    q[p] = qn;
+    dr = fma(dn, rho[p], dr);
+    dqn = fma(dn, qn, dqn);
+  }
+  block_sum2(dr, dqn);
+  if (threadIdx.x == 0) {
+    parts[2 * blockIdx.x] = dr;
+    parts[2 * blockIdx.x + 1] = dqn;
+  }
+}
+
+// alpha from the dots; x += alpha d, rho -= alpha q, r32 = float(rho); partials of rho . rho
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) k_fcg_step(Lvl<double> a, const double* d, const double* q, double* rho,
+                                                      float* r32, const double* parts_in, double* parts) {
+  double dr, dq;
+  totals2(parts_in, &dr, &dq);
+  const double alpha = dq != 0.0 ? dr / dq : 0.0;
+  double s = 0.0, unused = 0.0;
+  const long long n = npoints<DIM>(a);
+  for (long long t = blockIdx.x * (long long)kThreads + threadIdx.x; t < n; t += (long long)kBlocks * kThreads) {
+    long long p;
+    point<DIM>(a, t, &p);
+    a.phi[p] = fma(alpha, d[p], a.phi[p]);
+    const double r = fma(-alpha, q[p], rho[p]);
+    rho[p] = r;
+    if (r32) r32[p] = (float)r;
+    s = fma(r, r, s);
+  }
+  block_sum2(s, unused);
+  if (threadIdx.x == 0) parts[blockIdx.x] = s;
+}
+
+}  // namespace
+
+int fcg_num_parts() { return kBlocks; }
+
+void launch_fcg_init(int dim, const Lvl<double>& a, double* rho, double* d, double* q, float* r32, double* parts,
+                     cudaStream_t s) {
+  if (dim == 2) k_fcg_init<2><<<kBlocks, kThreads, 0, s>>>(a, rho, d, q, r32, parts);
+  else k_fcg_init<3><<<kBlocks, kThreads, 0, s>>>(a, rho, d, q, r32, parts);
+}
+
+template <typename TZ>
+void launch_fcg_iter(int dim, const Lvl<double>& a, const TZ* z, double* d, double* q, double* rho, float* r32,
+                     double* parts_dots, double* parts_dir, double* parts_res, cudaStream_t s) {
+  if (dim == 2) {
+    k_fcg_dots<2, TZ><<<kBlocks, kThreads, 0, s>>>(a, z, d, q, parts_dots);
+    k_fcg_dir<2, TZ><<<kBlocks, kThreads, 0, s>>>(a, z, d, q, rho, parts_dots, parts_dir);
+    k_fcg_step<2><<<kBlocks, kThreads, 0, s>>>(a, d, q, rho, r32, parts_dir, parts_res);
+  } else {
+    k_fcg_dots<3, TZ><<<kBlocks, kThreads, 0, s>>>(a, z, d, q, parts_dots);
+    k_fcg_dir<3, TZ><<<kBlocks, kThreads, 0, s>>>(a, z, d, q, rho, parts_dots, parts_dir);
+    k_fcg_step<3><<<kBlocks, kThreads, 0, s>>>(a, d, q, rho, r32, parts_dir, parts_res);
+  }
+}
+
+template void launch_fcg_iter<float>(int, const Lvl<double>&, const float*, double*, double*, double*, float*,
+                                     double*, double*, double*, cudaStream_t);
+template void launch_fcg_iter<double>(int, const Lvl<double>&, const double*, double*, double*, double*, float*,
+                                      double*, double*, double*, cudaStream_t);
+
+}  // namespace jmg

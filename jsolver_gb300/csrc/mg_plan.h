@@ -33,6 +33,11 @@ struct JmgPlan {
   bool mixed = false;
   std::vector<jmg::LevelInfo> lv;
   size_t off_phi_old = 0, off_state = 0, off_parts = 0, off_tab64 = 0, off_tab32 = 0, ws_bytes = 0;
+  // outer = FCG: FP64 level-0 vectors rho (residual), d (direction), q = L d, z64 (the
+  // FP64 cycle's output), three partial-sum arrays, and the FP64 level table whose level
+  // 0 is (z64, rho) for the cycle that preconditions
+  bool fcg = false;
+  size_t off_rho = 0, off_d = 0, off_q = 0, off_z64 = 0, off_fcg_parts = 0, off_tab64z = 0;
   int nparts = 0;
   // graph cache
   cudaGraphExec_t exec = nullptr;
@@ -48,7 +53,7 @@ struct JmgPlan {
   // global-memory kernel instead, from the first level of at most 8192 points)
   int cluster_ranks = 0;
   bool coarse_ready = false;  // coarse_setup done
-  bool force_block = false;   // JMG_COARSE=block at plan creation: no cluster kernel
+  bool force_block = true;    // single-block coarse kernel (JMG_COARSE=cluster at plan creation: cluster)
   jmg::ClusterLayout cluster{};
   size_t cluster_smem64 = 0, cluster_smem32 = 0;
 };

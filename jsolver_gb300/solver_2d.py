@@ -9,6 +9,9 @@ Extensions (keyword-only, defaults keep the reference's behaviour):
                                        relative residual ||rhs - L_h phi|| / ||rhs|| <= rtol
   precision='fp64'|'mixed'          -- FP32 cycles inside FP64 iterative refinement
   inner_cycles                      -- FP32 cycles per refinement step
+  outer='richardson'|'fcg'          -- iterate the cycle as the reference does, or use it
+                                       as the preconditioner of flexible CG (needs
+                                       stop='residual' or fixed=True)
   guess=None|'learned'|GuessNet     -- start from the learned network's prediction
                                        instead of phi (jsolver_gb300.learned)
 """
@@ -22,7 +25,8 @@ INT32_MAX = int(np.iinfo(np.int32).max)
 
 def solve_2d(grid_x, grid_y, phi, rhs, lam, D_xx, D_yy, *, D_xy=None, fixed=False, epsilon=1e-12, gamma=1,
              fcycle=False, skip_pre=False, nu1=1, nu2=1, max_iters_outer=INT32_MAX, max_iters_inner=INT32_MAX,
-             stop="distance", rtol=1e-10, precision="fp64", inner_cycles=1, guess=None):
+             stop="distance", rtol=1e-10, precision="fp64", inner_cycles=1, guess=None,
+             outer="richardson"):
     """Multigrid solve of div(D grad phi) - lam phi = rhs on a padded 2D grid.
 
     Reference: solve_2d (jsolver/solver_2d.py:196-236). Arrays have shape
@@ -32,7 +36,7 @@ def solve_2d(grid_x, grid_y, phi, rhs, lam, D_xx, D_yy, *, D_xy=None, fixed=Fals
     return _engine.solve((grid_x, grid_y), phi, rhs, lam, (D_xx, D_yy), D_xy, fixed=fixed, epsilon=epsilon,
                          gamma=gamma, fcycle=fcycle, skip_pre=skip_pre, nu1=nu1, nu2=nu2,
                          max_iters_outer=max_iters_outer, max_iters_inner=max_iters_inner, stop=stop, rtol=rtol,
-                         precision=precision, inner_cycles=inner_cycles, guess=guess)
+                         precision=precision, inner_cycles=inner_cycles, guess=guess, outer=outer)
 
 
 globals().update(make_wrappers(2, solve_2d))

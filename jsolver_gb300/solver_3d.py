@@ -14,7 +14,7 @@ INT32_MAX = int(np.iinfo(np.int32).max)
 
 def solve_3d(grid_x, grid_y, grid_z, phi, rhs, lam, D_xx, D_yy, D_zz, *, fixed=False, epsilon=1e-12, gamma=1,
              fcycle=False, skip_pre=False, nu1=1, nu2=1, max_iters_outer=INT32_MAX, max_iters_inner=INT32_MAX,
-             stop="distance", rtol=1e-10, precision="fp64", inner_cycles=1):
+             stop="distance", rtol=1e-10, precision="fp64", inner_cycles=1, outer="richardson"):
     """Multigrid solve on a padded 3D grid (jsolver/solver_3d.py:196-237).
 
     Arrays have shape (grid_z.mx + 3, grid_y.mx + 3, grid_x.mx + 3), float64. Returns
@@ -23,7 +23,7 @@ def solve_3d(grid_x, grid_y, grid_z, phi, rhs, lam, D_xx, D_yy, D_zz, *, fixed=F
     return _engine.solve((grid_x, grid_y, grid_z), phi, rhs, lam, (D_xx, D_yy, D_zz), None, fixed=fixed,
                          epsilon=epsilon, gamma=gamma, fcycle=fcycle, skip_pre=skip_pre, nu1=nu1, nu2=nu2,
                          max_iters_outer=max_iters_outer, max_iters_inner=max_iters_inner, stop=stop, rtol=rtol,
-                         precision=precision, inner_cycles=inner_cycles)
+                         precision=precision, inner_cycles=inner_cycles, outer=outer)
 
 
 globals().update(make_wrappers(3, solve_3d))

@@ -438,9 +438,9 @@ CLUSTER_CASES = [(2, 64, {}), (2, 256, {}), (2, 256, {"gamma": 2}), (2, 256, {"f
 @pytest.mark.parametrize("dim,m,form", CLUSTER_CASES,
                          ids=lambda x: ",".join(f"{k}={v}" for k, v in x.items()) if isinstance(x, dict) else str(x))
 def test_cluster_coarse_cycle_matches_single_block(dim, m, form, monkeypatch):
-    """The coarse levels on a thread-block cluster (rows spread over the CTAs' shared
-    memory) against the single-block global-memory kernel (JMG_COARSE=block): the same
-    point arithmetic, so the same phi to rounding and the same cycle count."""
+    """The coarse levels on a thread-block cluster (JMG_COARSE=cluster: rows spread over
+    the CTAs' shared memory) against the default single-block global-memory kernel: the
+    same point arithmetic, so the same phi to rounding and the same cycle count."""
     g = grid_1D(m)
     if dim == 2:
         p = W.random_2d(m, seed=21)
@@ -455,9 +455,47 @@ def test_cluster_coarse_cycle_matches_single_block(dim, m, form, monkeypatch):
         kw.update(stop="residual", rtol=1e-9)
     else:
         kw.update(fixed=True, max_iters_outer=5)
-    phi_c, c_c = fn(*grids, *args, **kw)
-    monkeypatch.setenv("JMG_COARSE", "block")
-    monkeypatch.setattr(_engine, "CACHE", _engine._Cache())
     phi_b, c_b = fn(*grids, *args, **kw)
+    monkeypatch.setenv("JMG_COARSE", "cluster")
+    monkeypatch.setattr(_engine, "CACHE", _engine._Cache())
+    phi_c, c_c = fn(*grids, *args, **kw)
     assert int(c_c) == int(c_b)
     assert rel_l2(phi_c, phi_b) < 1e-13, rel_l2(phi_c, phi_b)
+
+
+@pytest.mark.parametrize("dim,m,precision,form", [(2, 256, "fp64", {}), (2, 256, "mixed", {}), (2, 64, "fp64", {}),
+                                                  (2, 128, "mixed", {"gamma": 2}), (3, 32, "fp64", {"fcycle": True}),
+                                                  (3, 32, "mixed", {})])
+def test_fcg_outer_reaches_rtol(dim, m, precision, form):
+    """The cycle as the preconditioner of flexible CG (outer='fcg'): the true relative
+    residual (oracle, FP64 on the CPU) meets the tolerance up to the recurrence's drift,
+    in fewer cycles than the reference's stationary iteration, and the solution agrees
+    with the FP64 stationary one to the accuracy the tolerance allows."""
+    g = grid_1D(m)
+    if dim == 2:
+        p = W.random_2d(m, seed=9)
+        grids, fn = (g, g), solve_2d
+        args = (p["phi0"], p["rhs"], p["lam"], p["D_xx"], p["D_yy"])
+        o = mg2d.Oracle2D(g, g)
+    else:
+        p = W.random_3d(m, seed=9)
+        grids, fn = (g, g, g), solve_3d
+        args = (p["phi0"], p["rhs"], p["lam"], p["D_xx"], p["D_yy"], p["D_zz"])
+        o = mg3d.Oracle3D(g, g, g)
+    o.setup(*args)
+    ref, c_ref = fn(*grids, *args, stop="residual", rtol=1e-10, **form)
+    phi, c = fn(*grids, *args, stop="residual", rtol=1e-10, precision=precision, outer="fcg", **form)
+    rr = o.rel_residual(phi, p["rhs"])
+    assert rr <= 2e-10, rr
+    assert c < c_ref, (c, c_ref)
+    assert rel_l2(phi, ref) < 1e-6
+
+
+def test_fcg_outer_fixed_count_and_errors():
+    g = grid_1D(64)
+    p = W.random_2d(64, seed=2)
+    args = (p["phi0"], p["rhs"], p["lam"], p["D_xx"], p["D_yy"])
+    phi, c = solve_2d(g, g, *args, fixed=True, max_iters_outer=7, outer="fcg")
+    assert c == 7 and np.all(np.isfinite(phi))
+    with pytest.raises(ValueError, match="fcg"):
+        solve_2d(g, g, *args, outer="fcg")  # the distance stop measures a stationary iteration
