@@ -7,9 +7,10 @@ length 0.05), lambda ~ U[0, 10], rhs = L_h sin(pi x) sin(2 pi y).
 
 Forms (``--form``): ``fp64`` plain FP64 multigrid from phi0 = 0; ``mixed`` FP32 cycles in
 FP64 iterative refinement; ``learned`` / ``learned-mixed`` the same from the learned
-network's initial guess, whose computation is inside every timed step. The default
-(``auto``) is the headline form: learned-mixed in 2D (when the package holds trained
-weights), mixed in 3D. Every run also times the plain FP64 solve of the same problem
+network's initial guess, whose computation is inside every timed step. ``--outer``:
+``richardson`` iterates the cycle as the reference does; ``fcg`` uses the same cycle as
+the preconditioner of flexible CG. The default is the headline form, mixed precision
+with FCG; every run also times the reference's plain FP64 iteration of the same problem
 the same way and reports it under ``plain_fp64``.
 
 Our arm (default): ``value`` is the device time of a solve with inputs resident in HBM,
@@ -56,8 +57,9 @@ def parse():
     ap.add_argument("--form", default="auto", choices=["auto", "fp64", "mixed", "learned", "learned-mixed"])
     ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 comparison solve")
     ap.add_argument("--inner-cycles", type=int, default=1, help="FP32 cycles per refinement step (mixed forms)")
-    ap.add_argument("--outer", default="richardson", choices=["richardson", "fcg"],
-                    help="iterate the cycle (reference) or use it as the preconditioner of flexible CG")
+    ap.add_argument("--outer", default="auto", choices=["auto", "richardson", "fcg"],
+                    help="iterate the cycle (reference) or use it as the preconditioner of flexible CG; "
+                         "auto: fcg for the mixed and learned forms, richardson for fp64")
     ap.add_argument("--workload", default="2d", choices=sorted(WORKLOADS))
     ap.add_argument("--cycle", default=None, choices=["V", "W", "F"])
     ap.add_argument("--m", type=int, default=None)
@@ -70,8 +72,9 @@ def parse():
     a.m = a.m or m
     a.cycle = a.cycle or cyc
     if a.form == "auto":
-        from jsolver_gb300.learned import WEIGHTS
-        a.form = "learned-mixed" if dim == 2 and os.path.exists(WEIGHTS) else "mixed"
+        a.form = "mixed"
+    if a.outer == "auto":
+        a.outer = "richardson" if a.form == "fp64" else "fcg"
     return a
 
 

@@ -226,8 +226,10 @@ int jmg_net_inputs_2d(JmgNet* net, const JmgGrid* grid, const JmgCoeffs* coeffs,
 /* Training target of one problem: the block average of phi divided by out_scale * rms. */
 int jmg_net_target_2d(JmgNet* net, const JmgGrid* grid, const double* phi, const float* rms, float out_scale,
                       float* target, jmg_stream_t stream);
-/* phi0 (dense padded (m+3)^2 FP64) = out_scale * rms * the network output, bilinear
- * from the network grid to the solver grid, zero frame. */
+/* phi0 (dense padded (m+3)^2 FP64) = beta * out_scale * rms * the network output,
+ * bilinear from the network grid to the solver grid, zero frame; beta is the Ritz scale
+ * (g . rhs) / (g . L_h g) of that field g under the level-0 operator, the factor that
+ * minimises the energy-norm error (0 when it is not positive). */
 int jmg_net_guess_2d(JmgNet* net, const JmgGrid* grid, const JmgCoeffs* coeffs, const double* rhs, float out_scale,
                      double* phi0, jmg_stream_t stream);
 

@@ -207,6 +207,64 @@ __global__ void k_net_out(const float* y32, const float* rms, float out_scale, i
   }
 }
 
+// Ritz scale of the guess g: beta = (g . rhs) / (g . L g) minimises the energy-norm
+// error ||phi - beta g||_A for A = -L (SPD), L the level-0 operator built from the raw
+// coefficients as the solver builds it (2D face averages, solver_2d.py:341-416).
+// Partials per block: parts[2 b] = g . rhs, parts[2 b + 1] = g . L g (interior points).
+constexpr int kRitzBlocks = 304;
+__global__ void k_net_ritz_parts(const double* g, const double* rhs, int m, double idx2, double idy2, const double* lam,
+                                 double lam_s, const double* dxx, double dxx_s, const double* dyy, double dyy_s,
+                                 double* parts) {
+  const int w = m + 3, n = (m - 1) * (m - 1);
+  double a = 0.0, b = 0.0;
+  auto Dx = [&](size_t p) { return dxx ? dxx[p] : dxx_s; };
+  auto Dy = [&](size_t p) { return dyy ? dyy[p] : dyy_s; };
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int i = 2 + t % (m - 1), j = 2 + t / (m - 1);
+    const size_t p = (size_t)j * w + i;
+    const double ex = 0.5 * (Dx(p) + Dx(p + 1)) * idx2, wx = 0.5 * (Dx(p - 1) + Dx(p)) * idx2;
+    const double ny = 0.5 * (Dy(p) + Dy(p + w)) * idy2, sy = 0.5 * (Dy(p - w) + Dy(p)) * idy2;
+    const double cc = ex + wx + ny + sy + (lam ? lam[p] : lam_s);
+    const double lg = ex * g[p + 1] + wx * g[p - 1] + ny * g[p + w] + sy * g[p - w] - cc * g[p];
+    a = fma(g[p], rhs[p], a);
+    b = fma(g[p], lg, b);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  __shared__ double sa[32], sb[32];
+  if ((threadIdx.x & 31) == 0) {
+    sa[threadIdx.x >> 5] = a;
+    sb[threadIdx.x >> 5] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0, tb = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      ta += sa[k];
+      tb += sb[k];
+    }
+    parts[2 * blockIdx.x] = ta;
+    parts[2 * blockIdx.x + 1] = tb;
+  }
+}
+
+// g *= beta (beta from the partials, summed in a fixed order by every block)
+__global__ void k_net_ritz_scale(double* g, int n, const double* parts) {
+  __shared__ double beta;
+  if (threadIdx.x == 0) {
+    double a = 0, b = 0;
+    for (int k = 0; k < kRitzBlocks; ++k) {
+      a += parts[2 * k];
+      b += parts[2 * k + 1];
+    }
+    beta = (b != 0.0 && a / b > 0.0) ? a / b : 0.0;
+  }
+  __syncthreads();
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) g[t] *= beta;
+}
+
 // training target: block average of phi over the same f x f blocks as the inputs,
 // divided by out_scale * rms
 __global__ void k_net_target(const double* phi, const float* rms, float out_scale, int m, int f, int res,
@@ -247,6 +305,7 @@ struct JmgNet {
   float* tmp = nullptr;     // pooled input channels
   float* rms = nullptr;
   float* loss_scratch = nullptr;
+  double* ritz_parts = nullptr;
   std::vector<void*> allocs;
 
   template <typename T>
@@ -420,7 +479,8 @@ int jmg_net_create(JmgNet** out, int res, int max_batch) {
   }
   ok = ok && (n->y32 = n->alloc<float>(n->pix(0, B) * 16)) && (n->gy = n->alloc<bf16>(n->pix(0, B) * 16)) &&
        (n->x1 = n->alloc<bf16>(n->pix(0, 1) * 16)) && (n->tmp = n->alloc<float>(n->pix(0, 1) * 4)) &&
-       (n->rms = n->alloc<float>(1)) && (n->loss_scratch = n->alloc<float>(1));
+       (n->rms = n->alloc<float>(1)) && (n->loss_scratch = n->alloc<float>(1)) &&
+       (n->ritz_parts = n->alloc<double>(2 * kRitzBlocks));
   if (!ok) {
     jmg_net_destroy(n);
     return jmg::set_error_message(JMG_ERR_CUDA, "cudaMalloc failed while creating the network");
@@ -527,7 +587,13 @@ int jmg_net_guess_2d(JmgNet* n, const JmgGrid* grid, const JmgCoeffs* coeffs, co
   if (rc) return rc;
   forward(n, n->x1, 1, s);
   const int m = grid->m[0], R = n->res;
-  k_net_out<<<grid_for((size_t)(m + 3) * (m + 3)), 256, 0, s>>>(n->y32, n->rms, out_scale, m, m / R, R, phi0);
+  const int np = (m + 3) * (m + 3);
+  k_net_out<<<grid_for((size_t)np), 256, 0, s>>>(n->y32, n->rms, out_scale, m, m / R, R, phi0);
+  k_net_ritz_parts<<<kRitzBlocks, 256, 0, s>>>(phi0, rhs, m, grid->idel[0] * grid->idel[0],
+                                               grid->idel[1] * grid->idel[1], coeffs->lam, coeffs->lam_scalar,
+                                               coeffs->D[0], coeffs->D_scalar[0], coeffs->D[1], coeffs->D_scalar[1],
+                                               n->ritz_parts);
+  k_net_ritz_scale<<<grid_for((size_t)np), 256, 0, s>>>(phi0, np, n->ritz_parts);
   return cuda_check("jmg_net_guess_2d");
 }
 

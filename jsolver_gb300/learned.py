@@ -242,12 +242,12 @@ def sample_problems(n, m, seed, device, phi_kind="modes", modes=6):
 
 # ---- dataset, training, evaluation --------------------------------------------------------
 
-def solve_plain(g, prob, i, rtol=1e-10, precision="fp64", phi0=None):
+def solve_plain(g, prob, i, rtol=1e-10, precision="fp64", phi0=None, outer="richardson"):
     from .solver_2d import solve_2d
     rhs = prob["rhs"][i]
     p0 = torch.zeros_like(rhs) if phi0 is None else phi0
     return solve_2d(g, g, p0, rhs, prob["lam"][i], prob["D_xx"][i], prob["D_yy"][i], stop="residual", rtol=rtol,
-                    precision=precision)
+                    precision=precision, outer=outer)
 
 
 def build_dataset(net, n, m=256, seed=1, chunk=250, rtol=1e-8, log=print):
@@ -325,7 +325,8 @@ def val_mse(net, X, T, batch=32):
     return tot / cnt
 
 
-def evaluate(net, m, seeds, phi_kind="workload", rtol=1e-10, forms=("fp64", "mixed")):
+def evaluate(net, m, seeds, phi_kind="workload", rtol=1e-10,
+             forms=(("fp64", "richardson"), ("mixed", "richardson"), ("mixed", "fcg"))):
     """Cycles, solve times and initial residuals from the zero guess and from the
     learned guess on held-out problems (one problem per seed)."""
     g = grid_1D(m)
@@ -343,23 +344,24 @@ def evaluate(net, m, seeds, phi_kind="workload", rtol=1e-10, forms=("fp64", "mix
         row["guess_ms"] = ev0.elapsed_time(ev1)
         row["guess_rel_residual"] = rel_residual(g, phi0, rhs, lam, dxx, dyy)
         row["guess_rel_err"] = float((phi0 - prob["phi_exact"][0]).norm() / prob["phi_exact"][0].norm())
-        for form in forms:
+        for prec, outer in forms:
             for name, start in (("zero", None), ("learned", phi0)):
                 ev0.record()
                 if start is None:
-                    phi, cnt = solve_plain(g, prob, 0, rtol=rtol, precision=form)
+                    phi, cnt = solve_plain(g, prob, 0, rtol=rtol, precision=prec, outer=outer)
                 else:
                     phi0b = net.guess(g, g, rhs, lam, dxx, dyy)
-                    phi, cnt = solve_plain(g, prob, 0, rtol=rtol, precision=form, phi0=phi0b)
+                    phi, cnt = solve_plain(g, prob, 0, rtol=rtol, precision=prec, phi0=phi0b, outer=outer)
                 ev1.record()
                 ev1.synchronize()
-                row[f"{form}_{name}_cycles"] = int(cnt)
-                row[f"{form}_{name}_ms"] = ev0.elapsed_time(ev1)
+                row[f"{prec}-{outer}_{name}_cycles"] = int(cnt)
+                row[f"{prec}-{outer}_{name}_ms"] = ev0.elapsed_time(ev1)
         rows.append(row)
     return rows
 
 
 def rel_residual(g, phi, rhs, lam, dxx, dyy):
+    """||rhs - L_h phi|| / ||rhs|| (FP64, on the GPU) of one 2D problem."""
     from ._engine import OperatorSet
     ops = OperatorSet((g, g), lam, (dxx, dyy))
     return float(ops.rel_residual(phi, rhs))

@@ -206,3 +206,21 @@ def output_2d(y, rms, out_scale, m):
     out = np.zeros((m + 3, m + 3))
     out[2:m + 1, 2:m + 1] = phi[2:m + 1, 2:m + 1]
     return out
+
+
+def ritz_scale(g, rhs, lam, dxx, dyy, m):
+    """beta = (g . rhs) / (g . L g) over the interior, L the 2D level-0 operator with face
+    averages (the solver's), 0 when not positive (jmg_net_guess_2d's final scaling)."""
+    full = lambda v: np.broadcast_to(np.asarray(v, dtype=np.float64), rhs.shape)
+    Dx, Dy, lm = full(dxx), full(dyy), full(lam)
+    s2 = float(m) ** 2
+    i = slice(2, m + 1)
+    ex = 0.5 * (Dx[i, 2:m + 1] + Dx[i, 3:m + 2]) * s2
+    wx = 0.5 * (Dx[i, 1:m] + Dx[i, 2:m + 1]) * s2
+    ny = 0.5 * (Dy[2:m + 1, i] + Dy[3:m + 2, i]) * s2
+    sy = 0.5 * (Dy[1:m, i] + Dy[2:m + 1, i]) * s2
+    cc = ex + wx + ny + sy + lm[i, i]
+    lg = ex * g[i, 3:m + 2] + wx * g[i, 1:m] + ny * g[3:m + 2, i] + sy * g[1:m, i] - cc * g[i, i]
+    a = float(np.sum(g[i, i] * rhs[i, i]))
+    b = float(np.sum(g[i, i] * lg))
+    return a / b if b != 0 and a / b > 0 else 0.0
