@@ -76,6 +76,9 @@ typedef struct JmgConfig {
   int32_t outer;           /* JMG_OUTER_RICHARDSON (reference: phi += cycle correction) or
                               JMG_OUTER_FCG (the cycle preconditions flexible CG; needs
                               JMG_STOP_RESIDUAL or fixed; no reference counterpart) */
+  int32_t off_diag;        /* 1: solves pass D_xy with array D (2D 9-point stencil,
+                              solver_2d.py:410-416); the workspace then holds the diagonal
+                              couplings. jmg_solve2d_f64 sets it from its coefficients. */
 } JmgConfig;
 
 /* Coefficients of one solve: lam, D_xx, D_yy (, D_zz) and optional D_xy. */

@@ -29,7 +29,7 @@ _OUTER = {"richardson": _lib.OUTER_RICHARDSON, "fcg": _lib.OUTER_FCG}
 
 def make_config(fixed=False, epsilon=1e-12, gamma=1, fcycle=False, skip_pre=False, nu1=1, nu2=1,
                 max_iters_outer=INT32_MAX, max_iters_inner=INT32_MAX, stop="distance", rtol=1e-10,
-                precision="fp64", inner_cycles=1, outer="richardson"):
+                precision="fp64", inner_cycles=1, outer="richardson", off_diag=False):
     c = _lib.default_config()
     c.fixed = int(bool(fixed))
     c.epsilon = float(epsilon)
@@ -51,6 +51,7 @@ def make_config(fixed=False, epsilon=1e-12, gamma=1, fcycle=False, skip_pre=Fals
     if outer not in _OUTER:
         raise ValueError(f"outer must be one of {sorted(_OUTER)}, got {outer!r}")
     c.outer = _OUTER[outer]
+    c.off_diag = int(bool(off_diag))
     return c
 
 
@@ -157,6 +158,10 @@ class Prepared:
                 self.coeffs.D[a] = None
                 self.coeffs.D_scalar[a] = scalar_value(D[a])
         self.coeffs.D_xy = None
+        if D_xy is not None and spatial:
+            t = to_device(D_xy, device)
+            self.keep.append(t)
+            self.coeffs.D_xy = t.data_ptr()
 
 
 def solve(grids, phi, rhs, lam, D, D_xy=None, guess=None, **opts):
@@ -166,12 +171,11 @@ def solve(grids, phi, rhs, lam, D, D_xy=None, guess=None, **opts):
     trained network) or a ``learned.GuessNet`` replaces phi's values by the network's
     prediction (2D square grids; phi still fixes the shape and dtype rules)."""
     ndim = len(grids)
-    cfg = make_config(**opts)
     grid = make_grid(grids)
-    plan = CACHE.plan(grid, cfg)  # grid checks first (Solver_2D.__init__)
+    CACHE.plan(grid, make_config(**opts))  # grid checks first (Solver_2D.__init__)
     sl, spatial, off = validate(ndim, phi, rhs, lam, D, D_xy, expected_shape(grids))
-    if off:
-        raise NotImplementedError("spatially varying D with D_xy (9-point stencil) is not implemented on the GPU yet")
+    cfg = make_config(off_diag=off, **opts)
+    plan = CACHE.plan(grid, cfg)
     torch_in = any(is_cuda_tensor(a) for a in [phi, rhs, lam] + list(D))
     wants_grad = torch.is_grad_enabled() and any(isinstance(a, torch.Tensor) and a.requires_grad
                                                  for a in [phi, rhs, lam] + list(D))
@@ -181,8 +185,9 @@ def solve(grids, phi, rhs, lam, D, D_xy=None, guess=None, **opts):
         if not cfg.fixed:
             raise ValueError("reverse-mode differentiation needs fixed=True, as in the reference "
                              "(its dynamic while_loop is not reverse-differentiable)")
-        if ndim != 2 or cfg.precision != _lib.PREC_FP64:
-            raise NotImplementedError("the hand-written adjoint covers the 2D FP64 fixed-mode solve")
+        if ndim != 2 or cfg.precision != _lib.PREC_FP64 or off or cfg.outer != _lib.OUTER_RICHARDSON:
+            raise NotImplementedError("the hand-written adjoint covers the 2D FP64 fixed-mode solve of the "
+                                      "5-point stencil (no D_xy), iterated as in the reference")
         from .adjoint import solve_2d_fixed_diff
         return solve_2d_fixed_diff(grids, phi, rhs, lam, D[0], D[1], **opts)
     device = pick_device(phi, rhs, lam, *D)
@@ -211,12 +216,10 @@ class OperatorSet:
     def __init__(self, grids, lam, D, D_xy=None, **opts):
         self.ndim = len(grids)
         self.grids = grids
-        self.cfg = make_config(**opts)
-        self.plan = _lib.Plan(make_grid(grids), self.cfg)
         sl, spatial, off = validate(self.ndim, np.zeros(expected_shape(grids)), np.zeros(expected_shape(grids)),
                                     lam, D, D_xy, expected_shape(grids))
-        if off:
-            raise NotImplementedError("D_xy (9-point stencil) is not implemented on the GPU yet")
+        self.cfg = make_config(off_diag=off, **opts)
+        self.plan = _lib.Plan(make_grid(grids), self.cfg)
         self.device = pick_device(lam, *D)
         self.prep = Prepared(self.ndim, self.device, lam, D, D_xy, sl, spatial)
         self.ws = torch.empty(max(self.plan.workspace_bytes, 1), dtype=torch.uint8, device=self.device)

@@ -26,7 +26,8 @@ class JmgConfig(ctypes.Structure):
                 ("skip_pre", ctypes.c_int32), ("nu1", ctypes.c_int32), ("nu2", ctypes.c_int32),
                 ("max_iters_outer", ctypes.c_int64), ("max_iters_inner", ctypes.c_int64),
                 ("epsilon", ctypes.c_double), ("stop", ctypes.c_int32), ("rtol", ctypes.c_double),
-                ("precision", ctypes.c_int32), ("inner_cycles", ctypes.c_int32), ("outer", ctypes.c_int32)]
+                ("precision", ctypes.c_int32), ("inner_cycles", ctypes.c_int32), ("outer", ctypes.c_int32),
+                ("off_diag", ctypes.c_int32)]
 
 
 class JmgCoeffs(ctypes.Structure):

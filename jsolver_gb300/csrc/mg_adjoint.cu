@@ -168,6 +168,8 @@ int jmg_solve_fixed_vjp(JmgPlan* p, const double* phi0, const double* rhs, const
   if (p->dim != 2) return fail(JMG_ERR_VALUE, "the adjoint is implemented for 2D solves");
   if (!p->cfg.fixed) return fail(JMG_ERR_VALUE, "reverse mode needs fixed mode (as in the reference)");
   if (p->mixed) return fail(JMG_ERR_VALUE, "the adjoint differentiates the FP64 method (precision fp64)");
+  if (p->off_diag) return fail(JMG_ERR_VALUE, "the adjoint covers the 5-point stencil (no D_xy)");
+  if (p->fcg) return fail(JMG_ERR_VALUE, "the adjoint differentiates the reference's iteration (outer richardson)");
   if ((rc = check_coeffs(p, c))) return rc;
   if (!c->lam || !c->D[0] || !c->D[1])
     return fail(JMG_ERR_VALUE, "the adjoint needs lambda, D_xx and D_yy as arrays (broadcast scalars first)");

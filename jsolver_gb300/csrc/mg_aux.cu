@@ -144,19 +144,21 @@ __device__ __forceinline__ double block_sum(double v) {
 
 // sum over interior points of d^2, d = rhs - L_h phi (phi == nullptr: d = rhs); with r32,
 // d is also stored as FP32 (the right-hand side of the next refinement step)
+// Interior rows (2D: j; 3D: (k, j)) are dealt to the blocks round-robin and the threads
+// of a block walk each row: one 32-bit division per row, fixed reduction order.
 template <typename T, int DIM>
 __global__ void k_residual_partials(Lvl<T> a, const T* phi, double* parts, float* r32) {
-  const int nx = a.mx - 1, ny = a.my - 1, nz = DIM == 3 ? a.mz - 1 : 1;
-  const long long n = (long long)nx * ny * nz;
+  const int ny = a.my - 1, nz = DIM == 3 ? a.mz - 1 : 1;
+  const int nrows = ny * nz;
   double acc = 0.0;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 2 + (int)(t % nx);
-    const int j = 2 + (int)((t / nx) % ny);
-    const int k = 2 + (int)(t / ((long long)nx * ny));
+  for (int r = blockIdx.x; r < nrows; r += gridDim.x)
+  for (int i = 2 + threadIdx.x; i <= a.mx; i += blockDim.x) {
+    const int k = DIM == 3 ? 2 + r / ny : 0;
+    const int j = 2 + (DIM == 3 ? r % ny : r);
     const long long p = DIM == 2 ? (long long)j * a.P + i : (long long)k * a.S + (long long)j * a.P + i;
     double d;
     if (phi == nullptr) d = (double)a.rhs[p];
-    else if (DIM == 2) d = (double)defect_point2d<T>(phi, a.rhs, a.wx, a.wy, a.acc, p, a.P);
+    else if (DIM == 2) d = (double)defect_point2d<T>(a, phi, p);
     else d = (double)defect_point3d<T>(phi, a.rhs, a.wx, a.wy, a.wz, a.acc, p, a.P, a.S);
     if (r32) r32[p] = (float)d;
     acc = fma(d, d, acc);
@@ -268,7 +270,7 @@ __global__ void k_dense_residual(Lvl<double> a, Box b, double* d) {
   const bool in = I >= 2 && I <= a.mx && J >= 2 && J <= a.my && (DIM == 2 || (K >= 2 && K <= a.mz));
   if (in) {
     const long long p = (long long)K * a.S + (long long)J * a.P + I;
-    v = DIM == 2 ? defect_point2d<double>(a.phi, a.rhs, a.wx, a.wy, a.acc, p, a.P)
+    v = DIM == 2 ? defect_point2d<double>(a, a.phi, p)
                  : defect_point3d<double>(a.phi, a.rhs, a.wx, a.wy, a.wz, a.acc, p, a.P, a.S);
   }
   d[((long long)K * b.ny + J) * b.nx + I] = v;
@@ -294,7 +296,7 @@ __global__ void k_residual_to_f32(Lvl<double> a, float* r32) {
   float v = 0.f;
   const bool in = I >= 2 && I <= a.mx && J >= 2 && J <= a.my && (DIM == 2 || (K >= 2 && K <= a.mz));
   if (in)
-    v = (float)(DIM == 2 ? defect_point2d<double>(a.phi, a.rhs, a.wx, a.wy, a.acc, p, a.P)
+    v = (float)(DIM == 2 ? defect_point2d<double>(a, a.phi, p)
                          : defect_point3d<double>(a.phi, a.rhs, a.wx, a.wy, a.wz, a.acc, p, a.P, a.S));
   r32[p] = v;
 }

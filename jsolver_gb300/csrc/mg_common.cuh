@@ -28,6 +28,13 @@ struct Lvl {
   T* wz;
   T* invd;
   T* acc;
+  // 2D with D_xy (9-point stencil): diagonal couplings of p with its SW, SE, NW and NE
+  // neighbours, the reference's A_ll, A_rl, A_lr, A_rr (solver_2d.py:410-416); nullptr
+  // without D_xy
+  T* xll;
+  T* xrl;
+  T* xlr;
+  T* xrr;
   int mx, my, mz;  // resolution per axis (interior indices 2..m)
   int P;           // row pitch in elements
   long long S;     // plane stride in elements (3D)
@@ -78,17 +85,52 @@ __device__ __forceinline__ T defect_point2d(const T* ph, const T* rhs, const T* 
   return d + rhs[p];
 }
 
+// Off-diagonal part of the 9-point stencil at p (D_xy present), in the reference's
+// order ((A_ll SW + A_rl SE) + A_lr NW) + A_rr NE (solver_2d.py:686-690, 638-641).
+template <typename T>
+__device__ __forceinline__ T offdiag2d(const Lvl<T>& a, const T* ph, long long p) {
+  const int P = a.P;
+  T o = a.xll[p] * ph[p - P - 1];
+  o = fma(a.xrl[p], ph[p - P + 1], o);
+  o = fma(a.xlr[p], ph[p + P - 1], o);
+  o = fma(a.xrr[p], ph[p + P + 1], o);
+  return o;
+}
+
+// Gauss-Seidel value with the level's full stencil (5-point, or 9-point with D_xy):
+// (N/S/E/W part - rhs + off-diagonal part) / A_cc (solver_2d.py:687-690)
+template <typename T>
+__device__ __forceinline__ T gs_point2d(const Lvl<T>& a, long long p) {
+  if (!a.xll) return gs_point2d<T>(a.phi, a.rhs, a.wx, a.wy, a.invd, p, a.P);
+  const int P = a.P;
+  T s = a.wy[p] * a.phi[p + P];
+  s = fma(a.wy[p - P], a.phi[p - P], s);
+  s = fma(a.wx[p], a.phi[p + 1], s);
+  s = fma(a.wx[p - 1], a.phi[p - 1], s);
+  s = s - a.rhs[p];
+  s = s + offdiag2d(a, a.phi, p);
+  return s * a.invd[p];
+}
+
+// Defect of phi (not necessarily a.phi) with the level's full stencil: the 5-point
+// defect minus the off-diagonal part (solver_2d.py:637-642).
+template <typename T>
+__device__ __forceinline__ T defect_point2d(const Lvl<T>& a, const T* ph, long long p) {
+  const T d = defect_point2d(ph, a.rhs, a.wx, a.wy, a.acc, p, a.P);
+  return a.xll ? d - offdiag2d(a, ph, p) : d;
+}
+
 // Coarse right-hand side at coarse interior point (J, I) from the fine defects at the
 // red points (solver_2d.py:644): 1/16 of the four diagonal neighbours + 1/4 centre.
 template <typename T>
 __device__ __forceinline__ T restrict_point2d(const Lvl<T>& f, int J, int I) {
   const int P = f.P;
   const long long c = (long long)(2 * J - 1) * P + (2 * I - 1);
-  const T dne = defect_point2d(f.phi, f.rhs, f.wx, f.wy, f.acc, c + P + 1, P);
-  const T dnw = defect_point2d(f.phi, f.rhs, f.wx, f.wy, f.acc, c + P - 1, P);
-  const T dse = defect_point2d(f.phi, f.rhs, f.wx, f.wy, f.acc, c - P + 1, P);
-  const T dsw = defect_point2d(f.phi, f.rhs, f.wx, f.wy, f.acc, c - P - 1, P);
-  const T dc = defect_point2d(f.phi, f.rhs, f.wx, f.wy, f.acc, c, P);
+  const T dne = defect_point2d(f, f.phi, c + P + 1);
+  const T dnw = defect_point2d(f, f.phi, c + P - 1);
+  const T dse = defect_point2d(f, f.phi, c - P + 1);
+  const T dsw = defect_point2d(f, f.phi, c - P - 1);
+  const T dc = defect_point2d(f, f.phi, c);
   const T s = ((dne + dnw) + dse) + dsw;
   return T(0.0625) * s + T(0.25) * dc;
 }

@@ -99,6 +99,8 @@ int validate_and_layout(JmgPlan* p) {
   p->levels = L;
   p->used = L - 1;
   p->mixed = p->cfg.precision == JMG_PREC_MIXED;
+  if (p->cfg.off_diag && d != 2) return set_err(JMG_ERR_VALUE, "off_diag (D_xy) is a 2D option");
+  p->off_diag = d == 2 && p->cfg.off_diag;
   p->lv.resize(p->used);
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -123,6 +125,9 @@ int validate_and_layout(JmgPlan* p) {
     li.wz = d == 3 ? take(b8) : 0;
     li.invd = take(b8);
     li.acc = take(b8);
+    for (int c = 0; c < 4; ++c) li.xd[c] = li.xd32[c] = 0;
+    if (p->off_diag)
+      for (int c = 0; c < 4; ++c) li.xd[c] = take(b8);
     for (int c = 0; c < 3; ++c) li.d[c] = (d == 3 && l >= 1) ? take(b8) : 0;
     if (p->mixed) {
       li.phi32 = take(b4);
@@ -132,6 +137,8 @@ int validate_and_layout(JmgPlan* p) {
       li.wz32 = d == 3 ? take(b4) : 0;
       li.invd32 = take(b4);
       li.acc32 = take(b4);
+      if (p->off_diag)
+        for (int c = 0; c < 4; ++c) li.xd32[c] = take(b4);
     }
   }
   p->off_phi_old = take(p->lv[0].elems * 8);
@@ -188,7 +195,7 @@ int jmg::coarse_setup(JmgPlan* p) {
   const size_t limit = 200 * 1024;
   p->cluster_ranks = 0;
   p->coarse_start = block_coarse_start(p);
-  if (!p->force_block && p->used <= kMaxLevels) {
+  if (!p->force_block && !p->off_diag && p->used <= kMaxLevels) {
     for (int ranks : {16, 8}) {
       int lev0 = -1;
       ClusterLayout lay;
@@ -219,8 +226,14 @@ int jmg::coarse_setup(JmgPlan* p) {
 
 Lvl<double> jmg::lvl64(const JmgPlan* p, void* ws, int l) {
   const LevelInfo& li = p->lv[l];
-  Lvl<double> a;
+  Lvl<double> a{};
   a.phi = ptr<double>(ws, li.phi);
+  if (p->off_diag) {
+    a.xll = ptr<double>(ws, li.xd[0]);
+    a.xrl = ptr<double>(ws, li.xd[1]);
+    a.xlr = ptr<double>(ws, li.xd[2]);
+    a.xrr = ptr<double>(ws, li.xd[3]);
+  }
   a.rhs = ptr<double>(ws, li.rhs);
   a.wx = ptr<double>(ws, li.wx);
   a.wy = ptr<double>(ws, li.wy);
@@ -239,8 +252,14 @@ namespace {
 }  // namespace
 Lvl<float> jmg::lvl32(const JmgPlan* p, void* ws, int l) {
   const LevelInfo& li = p->lv[l];
-  Lvl<float> a;
+  Lvl<float> a{};
   a.phi = ptr<float>(ws, li.phi32);
+  if (p->off_diag) {
+    a.xll = ptr<float>(ws, li.xd32[0]);
+    a.xrl = ptr<float>(ws, li.xd32[1]);
+    a.xlr = ptr<float>(ws, li.xd32[2]);
+    a.xrr = ptr<float>(ws, li.xd32[3]);
+  }
   a.rhs = ptr<float>(ws, li.rhs32);
   a.wx = ptr<float>(ws, li.wx32);
   a.wy = ptr<float>(ws, li.wy32);
@@ -334,7 +353,7 @@ void emit_cycle(const JmgPlan* p, LvlTable<T>& tab, const LvlTable<T>* dtab, con
 // starts with a sweep at level 0 from a zero guess (no zeroing pass), and one tiled FP64
 // kernel gives both the stopping test's residual and the next step's FP32 right-hand side.
 bool mixed_fused(const JmgPlan* p) {
-  return !p->fcg && p->mixed && p->dim == 2 && p->cfg.stop == JMG_STOP_RESIDUAL && !p->cfg.fixed && p->coarse_start > 0 &&
+  return !p->fcg && !p->off_diag && p->mixed && p->dim == 2 && p->cfg.stop == JMG_STOP_RESIDUAL && !p->cfg.fixed && p->coarse_start > 0 &&
          p->cfg.nu1 >= 1 && p->cfg.nu2 >= 1;
 }
 
@@ -354,7 +373,7 @@ int loop_mode(const JmgPlan* p) {
 void emit_fcg_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaStream_t s) {
   LoopState* st = ptr<LoopState>(ws, p->off_state);
   Lvl<double> l0 = lvl64(p, ws, 0);
-  CycleParams cp = cycle_params(p, false);
+  CycleParams cp = cycle_params(p, p->off_diag);
   double* fp = ptr<double>(ws, p->off_fcg_parts);
   const int np = fcg_num_parts();
   double* rho = ptr<double>(ws, p->off_rho);
@@ -397,7 +416,7 @@ void emit_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaStream
   LoopState* st = ptr<LoopState>(ws, p->off_state);
   double* parts = ptr<double>(ws, p->off_parts);
   Lvl<double> l0 = lvl64(p, ws, 0);
-  CycleParams cp = cycle_params(p, false);
+  CycleParams cp = cycle_params(p, p->off_diag);
   int nparts = p->nparts;
   if (p->fcg) {
     emit_fcg_body(p, ws, handle, s);
@@ -468,7 +487,7 @@ void emit_prologue(const JmgPlan* p, void* ws, unsigned long long handle, cudaSt
 
 long long body_launches(const JmgPlan* p) {
   long long n = 0;
-  CycleParams cp = cycle_params(p, false);
+  CycleParams cp = cycle_params(p, p->off_diag);
   if (p->fcg) {
     const int inner = p->cfg.inner_cycles > 0 ? p->cfg.inner_cycles : 1;
     const bool zero_first = p->coarse_start > 0 && p->cfg.nu1 >= 1;
@@ -558,6 +577,7 @@ HierInputs hier_inputs(const JmgPlan* p, const JmgCoeffs* c) {
     if (a < p->dim && c->D[a] == nullptr) ++nscalar;
   }
   in.scalar_D = nscalar == p->dim;
+  in.Dxy = (p->off_diag && !in.scalar_D) ? c->D_xy : nullptr;
   return in;
 }
 
@@ -570,8 +590,12 @@ int jmg::check_coeffs(const JmgPlan* p, const JmgCoeffs* c) {
   if (nscalar != 0 && nscalar != p->dim)
     return set_err(JMG_ERR_VALUE, "Shape mismatch: the D components must be all scalars or all arrays.");
   if (c->D_xy && p->dim == 3) return set_err(JMG_ERR_VALUE, "D_xy is a 2D argument");
-  if (c->D_xy && nscalar == 0)
-    return set_err(JMG_ERR_VALUE, "D_xy (9-point stencil) is not supported by this build");
+  // D_xy takes part only with array D (solver_2d.py:333: off_diag needs spatial D)
+  const bool uses = c->D_xy && nscalar == 0;
+  if (uses && !p->off_diag)
+    return set_err(JMG_ERR_VALUE, "D_xy with array D needs a plan created with cfg.off_diag = 1");
+  if (!uses && p->off_diag)
+    return set_err(JMG_ERR_VALUE, "a plan created with cfg.off_diag = 1 needs D_xy and array D");
   return JMG_OK;
 }
 namespace {
@@ -594,9 +618,10 @@ int jmg::build_hierarchy(JmgPlan* p, const JmgCoeffs* c, void* ws, cudaStream_t 
   const Box b0 = p->lv[0].box;
   for (int l = 0; l < p->used; ++l) {
     const LevelInfo& li = p->lv[l];
-    double sq[3];
+    double sq[3], idl[3];
     for (int a = 0; a < 3; ++a) {
       const double id = a < p->dim ? p->grid.idel[a] * std::pow(0.5, l) : 0.0;  // solver_2d.py:323
+      idl[a] = id;
       sq[a] = id * id;                                                         // solver_2d.py:395
     }
     double* dcur[3] = {nullptr, nullptr, nullptr};
@@ -609,7 +634,7 @@ int jmg::build_hierarchy(JmgPlan* p, const JmgCoeffs* c, void* ws, cudaStream_t 
         bprev = p->lv[l - 1].box;
       }
     }
-    launch_hierarchy_level(p->dim, l, lvl64(p, ws, l), li.box, b0, in, sq, dcur, dprev, bprev, s);
+    launch_hierarchy_level(p->dim, l, lvl64(p, ws, l), li.box, b0, in, idl, sq, dcur, dprev, bprev, s);
   }
   if (p->mixed) {
     for (int l = 0; l < p->used; ++l) {
@@ -621,6 +646,12 @@ int jmg::build_hierarchy(JmgPlan* p, const JmgCoeffs* c, void* ws, cudaStream_t 
       if (p->dim == 3) launch_convert_f32(li.box, a.wz, f.wz, s);
       launch_convert_f32(li.box, a.invd, f.invd, s);
       launch_convert_f32(li.box, a.acc, f.acc, s);
+      if (p->off_diag) {
+        launch_convert_f32(li.box, a.xll, f.xll, s);
+        launch_convert_f32(li.box, a.xrl, f.xrl, s);
+        launch_convert_f32(li.box, a.xlr, f.xlr, s);
+        launch_convert_f32(li.box, a.xrr, f.xrr, s);
+      }
     }
   }
   JMG_CUDA(cudaGetLastError());
@@ -779,8 +810,12 @@ static int solve_oneshot(int dim, const JmgGrid* grid, const JmgConfig* cfg, con
                          const JmgCoeffs* c, double* phi_out, int64_t* count_out, void* ws, size_t bytes,
                          jmg_stream_t stream) {
   if (!grid || grid->ndim != dim) return set_err(JMG_ERR_VALUE, "grid->ndim must be %d", dim);
+  if (!cfg || !c) return set_err(JMG_ERR_VALUE, "NULL argument");
+  // the one-shot form sets off_diag itself: D_xy with array D selects the 9-point stencil
+  JmgConfig cf = *cfg;
+  cf.off_diag = dim == 2 && c->D_xy && c->D[0] && c->D[1] ? 1 : 0;
   JmgPlan* p = nullptr;
-  int rc = jmg_plan_create(&p, grid, cfg);
+  int rc = jmg_plan_create(&p, grid, &cf);
   if (rc) return rc;
   rc = jmg_solve(p, phi0, rhs, c, phi_out, count_out, ws, bytes, stream);
   if (rc == JMG_OK && p->exec) {
@@ -848,7 +883,7 @@ int jmg_op_prolong(JmgPlan* p, int level, double* phi, const double* phi_c, void
   Lvl<double> f = lvl64(p, ws, level), c = lvl64(p, ws, level + 1);
   launch_copy_in(p->lv[level].box, phi, f.phi, 0, s);
   launch_copy_in(p->lv[level + 1].box, phi_c, c.phi, 0, s);
-  launch_prolong<double>(p->dim, f, c, cycle_params(p, false).diag, s);
+  launch_prolong<double>(p->dim, f, c, cycle_params(p, p->off_diag).diag, s);
   launch_copy_out(p->lv[level].box, f.phi, phi, s);
   JMG_CUDA(cudaGetLastError());
   return JMG_OK;

@@ -30,6 +30,7 @@ struct HierArgs {
   const double* lam;
   double lam_s;
   double sq[3];    // idel_l^2 per axis
+  double cxy;      // 2D with D_xy: idel_x,l * idel_y,l * 0.25 (solver_2d.py:410)
   double* dcur[3];        // 3D: averaged D of this level (level >= 1)
   const double* dprev[3]; // 3D: averaged D of level-1 (level-1 >= 1)
 };
@@ -104,6 +105,32 @@ __global__ void k_hier_diag2d(HierArgs h) {
   }
   h.a.acc[p] = acc;
   h.a.invd[p] = inv;
+}
+
+// 2D with D_xy: the diagonal couplings of level l from the raw injected D_xy (no face
+// averaging for D_xy), on J, I in 1..m+1 (solver_2d.py:352-356, 410-416):
+//   A_ll = (Dxy[J][I-1] + Dxy[J-1][I]) c      A_lr = -(Dxy[J][I-1] + Dxy[J+1][I]) c
+//   A_rl = -(Dxy[J][I+1] + Dxy[J-1][I]) c     A_rr = (Dxy[J][I+1] + Dxy[J+1][I]) c
+// with c = idel_x * idel_y * 0.25 and D_xy in slot 2 of h.D.
+__global__ void k_hier_xy2d(HierArgs h) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  if (I >= h.b.nx || J >= h.b.ny) return;
+  const int mx = h.b.nx - 3, my = h.b.ny - 3;
+  const long long p = (long long)J * h.b.P + I;
+  double ll = 0.0, lr = 0.0, rl = 0.0, rr = 0.0;
+  if (J >= 1 && J <= my + 1 && I >= 1 && I <= mx + 1) {
+    const double w = raw2d(h, 2, J, I - 1), e = raw2d(h, 2, J, I + 1);
+    const double sth = raw2d(h, 2, J - 1, I), nth = raw2d(h, 2, J + 1, I);
+    ll = __dmul_rn(__dadd_rn(w, sth), h.cxy);
+    lr = __dmul_rn(-__dadd_rn(w, nth), h.cxy);
+    rl = __dmul_rn(-__dadd_rn(e, sth), h.cxy);
+    rr = __dmul_rn(__dadd_rn(e, nth), h.cxy);
+  }
+  h.a.xll[p] = ll;
+  h.a.xlr[p] = lr;
+  h.a.xrl[p] = rl;
+  h.a.xrr[p] = rr;
 }
 
 // 3D: source of level l's injection for component c at coarse (K, J, I) in 1..m+1
@@ -181,7 +208,7 @@ __global__ void k_hier_diag3d(HierArgs h) {
 static inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
 void launch_hierarchy_level(int dim, int level, const Lvl<double>& a, const Box& b, const Box& b0,
-                            const HierInputs& in, const double* sq_idel, double* const* d_cur,
+                            const HierInputs& in, const double* idel, const double* sq_idel, double* const* d_cur,
                             const double* const* d_prev, const Box& bprev, cudaStream_t s) {
   HierArgs h;
   h.a = a;
@@ -201,10 +228,16 @@ void launch_hierarchy_level(int dim, int level, const Lvl<double>& a, const Box&
   }
   h.lam = in.lam;
   h.lam_s = in.lam_scalar;
+  h.cxy = 0.0;
   dim3 blk(32, 8, 1), grd(cdiv(b.nx, 32), cdiv(b.ny, 8), dim == 3 ? b.nz : 1);
   if (dim == 2) {
     k_hier_faces2d<<<grd, blk, 0, s>>>(h);
     k_hier_diag2d<<<grd, blk, 0, s>>>(h);
+    if (a.xll && in.Dxy) {
+      h.D[2] = in.Dxy;
+      h.cxy = (idel[0] * idel[1]) * 0.25;
+      k_hier_xy2d<<<grd, blk, 0, s>>>(h);
+    }
   } else {
     k_hier_faces3d<<<grd, blk, 0, s>>>(h);
     k_hier_diag3d<<<grd, blk, 0, s>>>(h);

@@ -21,15 +21,19 @@ namespace jmg {
 // 2D: blockDim (64, 4); x walks the points of one colour in a row, y walks rows. With
 // zero_other, the other colour is taken as zero without being read: the first colour
 // pass of a sweep from a zero initial guess (a refinement step's correction).
+// With D_xy the two sub-lattices of a colour neighbour each other diagonally, so the
+// reference's order matters: row_par >= 0 restricts the pass to the rows of that parity
+// (one sub-lattice), and four passes make a sweep (solver_2d.py:684).
 template <typename T>
-__global__ void k_sweep_color2d(Lvl<T> a, int color, int zero_other) {
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
+__global__ void k_sweep_color2d(Lvl<T> a, int color, int zero_other, int row_par) {
+  const int r = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i = row_par < 0 ? r + 2 : 2 + row_par + 2 * r;
   if (i > a.my) return;
   const int j = 2 + ((i + color) & 1) + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
   if (j > a.mx) return;
   const long long p = (long long)i * a.P + j;
   // with all neighbours zero, (0 - rhs) / A_cc is what the full expression gives
-  a.phi[p] = zero_other ? (T(0) - a.rhs[p]) * a.invd[p] : gs_point2d<T>(a.phi, a.rhs, a.wx, a.wy, a.invd, p, a.P);
+  a.phi[p] = zero_other ? (T(0) - a.rhs[p]) * a.invd[p] : gs_point2d<T>(a, p);
 }
 
 // 3D: blockDim (64, 4, 1); grid z walks planes.
@@ -110,12 +114,29 @@ __device__ void blk_sweep(const Lvl<T>& a) {
       const int hx = a.mx / 2;  // points of one colour per row (m even) -- m >= 2
       const int rows = a.my - 1;
       const int n = hx * rows;
-      for (int t = threadIdx.x; t < n; t += nt) {
-        const int i = 2 + t / hx;
-        const int j = 2 + ((i + color) & 1) + 2 * (t % hx);
-        if (j > a.mx) continue;
-        const long long p = (long long)i * a.P + j;
-        a.phi[p] = gs_point2d<T>(a.phi, a.rhs, a.wx, a.wy, a.invd, p, a.P);
+      if (a.xll) {
+        // 9-point stencil: the colour's two sub-lattices in the reference's order, rows
+        // of parity 1 then 0 for red, 0 then 1 for black (solver_2d.py:684)
+        for (int half = 0; half < 2; ++half) {
+          const int rp = color == 0 ? 1 - half : half;
+          for (int t = threadIdx.x; t < n; t += nt) {
+            const int i = 2 + t / hx;
+            if ((i & 1) != rp) continue;
+            const int j = 2 + ((i + color) & 1) + 2 * (t % hx);
+            if (j > a.mx) continue;
+            const long long p = (long long)i * a.P + j;
+            a.phi[p] = gs_point2d<T>(a, p);
+          }
+          if (half == 0) __syncthreads();
+        }
+      } else {
+        for (int t = threadIdx.x; t < n; t += nt) {
+          const int i = 2 + t / hx;
+          const int j = 2 + ((i + color) & 1) + 2 * (t % hx);
+          if (j > a.mx) continue;
+          const long long p = (long long)i * a.P + j;
+          a.phi[p] = gs_point2d<T>(a.phi, a.rhs, a.wx, a.wy, a.invd, p, a.P);
+        }
       }
     } else {
       const int hx = a.mx / 2;
@@ -247,11 +268,22 @@ static inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b
 // from phi = 0 (the red pass does not read phi). a.phi holds the result on return.
 template <typename T>
 void launch_sweep(int dim, Lvl<T>& a, cudaStream_t s, bool zero_init) {
+  if (dim == 2 && a.xll) {
+    // 9-point stencil: sub-lattices (0,0), (1,1), (0,1), (1,0) of the reference
+    // (odd/odd, even/even, even-row/odd-column, odd-row/even-column), one pass each
+    if (zero_init) cudaMemsetAsync(a.phi, 0, (size_t)a.P * (a.my + 3) * sizeof(T), s);
+    const int colour[4] = {0, 0, 1, 1}, rpar[4] = {1, 0, 0, 1};
+    for (int q = 0; q < 4; ++q) {
+      dim3 b(64, 4), g(cdiv(a.mx / 2, 64), cdiv((a.my - 1 + 1) / 2, 4));
+      k_sweep_color2d<T><<<g, b, 0, s>>>(a, colour[q], 0, rpar[q]);
+    }
+    return;
+  }
   for (int color = 0; color < 2; ++color) {
     const int zero = (zero_init && color == 0) ? 1 : 0;
     if (dim == 2) {
       dim3 b(64, 4), g(cdiv(a.mx / 2, 64), cdiv(a.my - 1, 4));
-      k_sweep_color2d<T><<<g, b, 0, s>>>(a, color, zero);
+      k_sweep_color2d<T><<<g, b, 0, s>>>(a, color, zero, -1);
     } else {
       dim3 b(64, 4, 1), g(cdiv(a.mx / 2, 64), cdiv(a.my - 1, 4), a.mz - 1);
       k_sweep_color3d<T><<<g, b, 0, s>>>(a, color, zero);
@@ -261,8 +293,11 @@ void launch_sweep(int dim, Lvl<T>& a, cudaStream_t s, bool zero_init) {
 
 template <typename T>
 void launch_restrict(int dim, const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s) {
-  if (dim == 2) {
+  if (dim == 2 && !f.xll) {
     launch_restrict_tile2d<T>(f, c, s);
+  } else if (dim == 2) {
+    dim3 b(32, 8), g(cdiv(c.mx + 3, 32), cdiv(c.my + 3, 8));
+    k_restrict2d<T><<<g, b, 0, s>>>(f, c);
   } else {
     dim3 b(32, 8, 1), g(cdiv(c.mx + 3, 32), cdiv(c.my + 3, 8), c.mz + 3);
     k_restrict3d<T><<<g, b, 0, s>>>(f, c);

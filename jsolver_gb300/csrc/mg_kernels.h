@@ -119,11 +119,12 @@ struct HierInputs {
   const double* D[3]; double D_scalar[3];
   int scalar_D;     // all D components scalar
   int scalar_lam;
+  const double* Dxy = nullptr;  // 2D off-diagonal D (array D only), or nullptr
 };
 // Builds wx, wy, (wz), acc, invd of level l (and the averaged D arrays of level l in 3D).
 // dprev: averaged D of level l-1 (3D, l >= 2), or nullptr.
 void launch_hierarchy_level(int dim, int level, const Lvl<double>& a, const Box& b, const Box& b0,
-                            const HierInputs& in, const double* sq_idel, double* const* d_cur,
+                            const HierInputs& in, const double* idel, const double* sq_idel, double* const* d_cur,
                             const double* const* d_prev, const Box& bprev, cudaStream_t s);
 
 }  // namespace jmg

@@ -68,21 +68,24 @@ __device__ __forceinline__ void totals2(const double* parts, double* t0, double*
   *t1 = s[1];
 }
 
+// Interior rows (2D: j; 3D: (k, j)) are dealt to the kBlocks blocks round-robin, and the
+// threads of a block walk each row in x: one 32-bit division per row instead of 64-bit
+// index arithmetic per point. The reduction order stays fixed.
 template <int DIM>
-__device__ __forceinline__ bool point(const Lvl<double>& a, long long t, long long* p) {
-  const int nx = a.mx - 1, ny = a.my - 1, nz = DIM == 3 ? a.mz - 1 : 1;
-  if (t >= (long long)nx * ny * nz) return false;
-  const int i = 2 + (int)(t % nx);
-  const int j = 2 + (int)((t / nx) % ny);
-  const int k = 2 + (int)(t / ((long long)nx * ny));
-  *p = DIM == 2 ? (long long)j * a.P + i : (long long)k * a.S + (long long)j * a.P + i;
-  return true;
+__device__ __forceinline__ int nrows(const Lvl<double>& a) {
+  return (a.my - 1) * (DIM == 3 ? a.mz - 1 : 1);
 }
-
 template <int DIM>
-__device__ __forceinline__ long long npoints(const Lvl<double>& a) {
-  return (long long)(a.mx - 1) * (a.my - 1) * (DIM == 3 ? a.mz - 1 : 1);
+__device__ __forceinline__ long long row_base(const Lvl<double>& a, int r) {
+  const int k = DIM == 3 ? 2 + r / (a.my - 1) : 0;
+  const int j = 2 + (DIM == 3 ? r % (a.my - 1) : r);
+  return DIM == 2 ? (long long)j * a.P : (long long)k * a.S + (long long)j * a.P;
 }
+#define JMG_FOR_POINTS(a, p)                                                          \
+  for (int r_ = blockIdx.x; r_ < nrows<DIM>(a); r_ += kBlocks)                        \
+    for (long long base_ = row_base<DIM>(a, r_), i_ = 2 + threadIdx.x; i_ <= (a).mx; \
+         i_ += kThreads)                                                              \
+      if (const long long p = base_ + i_; true)
 
 // L z at p (FP64 arithmetic on z's values): -(A_cc z - sum of couplings * neighbours),
 // in the order of the defect (mg_common.cuh: defect_point2d/3d)
@@ -97,6 +100,14 @@ __device__ __forceinline__ double apply_L(const Lvl<double>& a, const TZ* z, lon
     t = fma(-a.wz[p - a.S], (double)z[p - a.S], t);
     t = fma(-a.wz[p], (double)z[p + a.S], t);
   }
+  if (DIM == 2 && a.xll) {  // 9-point stencil (D_xy): the off-diagonal couplings
+    const int P = a.P;
+    double o = a.xll[p] * (double)z[p - P - 1];
+    o = fma(a.xrl[p], (double)z[p - P + 1], o);
+    o = fma(a.xlr[p], (double)z[p + P - 1], o);
+    o = fma(a.xrr[p], (double)z[p + P + 1], o);
+    t = t - o;
+  }
   return -t;
 }
 
@@ -105,11 +116,8 @@ template <int DIM>
 __global__ void __launch_bounds__(kThreads) k_fcg_init(Lvl<double> a, double* rho, double* d, double* q, float* r32,
                                                       double* parts) {
   double s = 0.0, unused = 0.0;
-  const long long n = npoints<DIM>(a);
-  for (long long t = blockIdx.x * (long long)kThreads + threadIdx.x; t < n; t += (long long)kBlocks * kThreads) {
-    long long p;
-    point<DIM>(a, t, &p);
-    const double r = DIM == 2 ? defect_point2d<double>(a.phi, a.rhs, a.wx, a.wy, a.acc, p, a.P)
+  JMG_FOR_POINTS(a, p) {
+    const double r = DIM == 2 ? defect_point2d<double>(a, a.phi, p)
                               : defect_point3d<double>(a.phi, a.rhs, a.wx, a.wy, a.wz, a.acc, p, a.P, a.S);
     rho[p] = r;
     d[p] = 0.0;
@@ -126,10 +134,7 @@ template <int DIM, typename TZ>
 __global__ void __launch_bounds__(kThreads) k_fcg_dots(Lvl<double> a, const TZ* z, const double* d, const double* q,
                                                       double* parts) {
   double zq = 0.0, dq = 0.0;
-  const long long n = npoints<DIM>(a);
-  for (long long t = blockIdx.x * (long long)kThreads + threadIdx.x; t < n; t += (long long)kBlocks * kThreads) {
-    long long p;
-    point<DIM>(a, t, &p);
+  JMG_FOR_POINTS(a, p) {
     const double qp = q[p];
     zq = fma((double)z[p], qp, zq);
     dq = fma(d[p], qp, dq);
@@ -149,10 +154,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_dir(Lvl<double> a, const TZ* z
   totals2(parts_in, &zq, &dq);
   const double beta = dq != 0.0 ? zq / dq : 0.0;
   double dr = 0.0, dqn = 0.0;
-  const long long n = npoints<DIM>(a);
-  for (long long t = blockIdx.x * (long long)kThreads + threadIdx.x; t < n; t += (long long)kBlocks * kThreads) {
-    long long p;
-    point<DIM>(a, t, &p);
+  JMG_FOR_POINTS(a, p) {
     const double dn = fma(-beta, d[p], (double)z[p]);
     const double qn = fma(-beta, q[p], apply_L<DIM, TZ>(a, z, p));
     d[p] = dn;
@@ -175,10 +177,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_step(Lvl<double> a, const doub
   totals2(parts_in, &dr, &dq);
   const double alpha = dq != 0.0 ? dr / dq : 0.0;
   double s = 0.0, unused = 0.0;
-  const long long n = npoints<DIM>(a);
-  for (long long t = blockIdx.x * (long long)kThreads + threadIdx.x; t < n; t += (long long)kBlocks * kThreads) {
-    long long p;
-    point<DIM>(a, t, &p);
+  JMG_FOR_POINTS(a, p) {
     a.phi[p] = fma(alpha, d[p], a.phi[p]);
     const double r = fma(-alpha, q[p], rho[p]);
     rho[p] = r;

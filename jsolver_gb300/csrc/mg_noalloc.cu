@@ -86,7 +86,8 @@ int jmg_rel_residual_noalloc(const JmgGrid* grid, const double* phi, const doubl
   if (nscalar != 0 && nscalar != dim)
     return noalloc_err(JMG_ERR_VALUE, "Shape mismatch: the D components must be all scalars or all arrays.");
   if (coeffs->D_xy && nscalar == 0)
-    return noalloc_err(JMG_ERR_VALUE, "D_xy (9-point stencil) is not supported by this build");
+    return noalloc_err(JMG_ERR_VALUE, "jmg_rel_residual_noalloc takes no D_xy: its fixed scratch holds the "
+                                      "5-point coefficients only; use jmg_rel_residual");
 
   // dense padded layout of the caller's arrays
   Box b;
@@ -113,7 +114,7 @@ int jmg_rel_residual_noalloc(const JmgGrid* grid, const double* phi, const doubl
   int rc = scratch_for_current_device(&scratch);
   if (rc != JMG_OK) return rc;
 
-  Lvl<double> a;
+  Lvl<double> a{};
   a.phi = const_cast<double*>(phi);
   a.rhs = const_cast<double*>(rhs);
   a.wx = scratch;
@@ -138,12 +139,15 @@ int jmg_rel_residual_noalloc(const JmgGrid* grid, const double* phi, const doubl
     in.D_scalar[k] = k < dim ? coeffs->D_scalar[k] : 0.0;
   }
   in.scalar_D = nscalar == dim;
-  double sq[3] = {0, 0, 0};
-  for (int k = 0; k < dim; ++k) sq[k] = grid->idel[k] * grid->idel[k];
+  double sq[3] = {0, 0, 0}, idl[3] = {0, 0, 0};
+  for (int k = 0; k < dim; ++k) {
+    idl[k] = grid->idel[k];
+    sq[k] = grid->idel[k] * grid->idel[k];
+  }
 
   cudaStream_t s = (cudaStream_t)stream;
   // level-0 coefficients over the whole box (every scratch value read below is written here)
-  launch_hierarchy_level(dim, 0, a, b, b, in, sq, nullptr, nullptr, b, s);
+  launch_hierarchy_level(dim, 0, a, b, b, in, idl, sq, nullptr, nullptr, b, s);
   launch_residual_partials<double>(dim, a, nullptr, parts, nparts, s);
   launch_rhs_norm(st, parts, nparts, s);
   launch_residual_partials<double>(dim, a, a.phi, parts, nparts, s);

@@ -19,6 +19,7 @@ struct LevelInfo {
   size_t phi, rhs, wx, wy, wz, invd, acc;   // FP64 arrays (byte offsets)
   size_t d[3];                              // 3D averaged D (levels >= 1)
   size_t phi32, rhs32, wx32, wy32, wz32, invd32, acc32;  // FP32 mirrors (mixed precision)
+  size_t xd[4], xd32[4];  // 2D with D_xy: A_ll, A_rl, A_lr, A_rr (FP64, FP32 mirrors); 0 if absent
 };
 
 }  // namespace jmg
@@ -31,6 +32,7 @@ struct JmgPlan {
   int used = 0;         // levels visited: 0..L-2
   int coarse_start = 0; // first level run by one coarse sub-cycle kernel
   bool mixed = false;
+  bool off_diag = false;  // 2D 9-point stencil (D_xy)
   std::vector<jmg::LevelInfo> lv;
   size_t off_phi_old = 0, off_state = 0, off_parts = 0, off_tab64 = 0, off_tab32 = 0, ws_bytes = 0;
   // outer = FCG: FP64 level-0 vectors rho (residual), d (direction), q = L d, z64 (the
