@@ -86,6 +86,7 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 
 __global__ void k_distance_snapshot(Box b, double* __restrict__ old_phi, const double* __restrict__ phi,
                                     LoopState* st) {
+  pdl_enter();
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
   const int K = blockIdx.z;
@@ -111,7 +112,7 @@ __global__ void k_distance_snapshot(Box b, double* __restrict__ old_phi, const d
 
 void launch_distance_snapshot(const Box& b, double* old_phi, const double* phi, LoopState* st, cudaStream_t s) {
   dim3 blk(32, 8, 1), g(cdiv(b.nx, 32), cdiv(b.ny, 8), b.nz);
-  k_distance_snapshot<<<g, blk, 0, s>>>(b, old_phi, phi, st);
+  launch_k(k_distance_snapshot, g, blk, 0, s, b, old_phi, phi, st);
 }
 
 // ------------------------------------------------------------------------------------
@@ -148,6 +149,7 @@ __device__ __forceinline__ double block_sum(double v) {
 // of a block walk each row: one 32-bit division per row, fixed reduction order.
 template <typename T, int DIM>
 __global__ void k_residual_partials(Lvl<T> a, const T* phi, double* parts, float* r32) {
+  pdl_enter();
   const int ny = a.my - 1, nz = DIM == 3 ? a.mz - 1 : 1;
   const int nrows = ny * nz;
   double acc = 0.0;
@@ -171,9 +173,9 @@ template <typename T>
 void launch_residual_partials(int dim, const Lvl<T>& a, const T* phi_or_null, double* parts, int, cudaStream_t s,
                               float* r32) {
   if (dim == 2)
-    k_residual_partials<T, 2><<<kResBlocks, kResThreads, 0, s>>>(a, phi_or_null, parts, r32);
+    launch_k(k_residual_partials<T, 2>, dim3(kResBlocks), dim3(kResThreads), 0, s, a, phi_or_null, parts, r32);
   else
-    k_residual_partials<T, 3><<<kResBlocks, kResThreads, 0, s>>>(a, phi_or_null, parts, r32);
+    launch_k(k_residual_partials<T, 3>, dim3(kResBlocks), dim3(kResThreads), 0, s, a, phi_or_null, parts, r32);
 }
 template void launch_residual_partials<double>(int, const Lvl<double>&, const double*, double*, int, cudaStream_t,
                                                float*);
@@ -209,6 +211,7 @@ __global__ void k_loop_init(LoopState* st, const double* parts, int nparts, int 
 
 __global__ void k_loop_step(LoopState* st, const double* parts, int nparts, int mode, double eps, double rtol,
                             long long max_iters, unsigned long long handle) {
+  pdl_enter();
   double r = 0.0;
   if (mode == 1) r = sqrt(reduce_parts_warp(parts, nparts));
   if (threadIdx.x != 0) return;
@@ -246,7 +249,7 @@ void launch_loop_init(LoopState* st, const double* parts, int nparts, int mode, 
 }
 void launch_loop_step(LoopState* st, const double* parts, int nparts, int mode, double eps, double rtol,
                       long long max_iters, unsigned long long h, cudaStream_t s) {
-  k_loop_step<<<1, 32, 0, s>>>(st, parts, nparts, mode, eps, rtol, max_iters, h);
+  launch_k(k_loop_step, dim3(1), dim3(32), 0, s, st, parts, nparts, mode, eps, rtol, max_iters, h);
 }
 void launch_rhs_norm(LoopState* st, const double* parts, int nparts, cudaStream_t s) {
   k_rhs_norm<<<1, 32, 0, s>>>(st, parts, nparts);
@@ -309,6 +312,7 @@ void launch_residual_to_f32(int dim, const Lvl<double>& a, float* r32, cudaStrea
 
 template <int DIM>
 __global__ void k_add_correction(Lvl<double> a, const float* e32) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
   const int k = blockIdx.z + 2;
@@ -319,8 +323,8 @@ __global__ void k_add_correction(Lvl<double> a, const float* e32) {
 
 void launch_add_correction(int dim, const Lvl<double>& a, const float* e32, cudaStream_t s) {
   dim3 blk(64, 4, 1), g(cdiv(a.mx - 1, 64), cdiv(a.my - 1, 4), dim == 3 ? a.mz - 1 : 1);
-  if (dim == 2) k_add_correction<2><<<g, blk, 0, s>>>(a, e32);
-  else k_add_correction<3><<<g, blk, 0, s>>>(a, e32);
+  if (dim == 2) launch_k(k_add_correction<2>, g, blk, 0, s, a, e32);
+  else launch_k(k_add_correction<3>, g, blk, 0, s, a, e32);
 }
 
 __global__ void k_convert_f32(Box b, const double* src, float* dst) {

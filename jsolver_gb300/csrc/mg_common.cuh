@@ -42,6 +42,19 @@ struct Lvl {
 
 constexpr int kMaxLevels = 16;
 
+// Programmatic dependent launch (PDL). Kernels of the cycle are launched with
+// programmatic stream serialisation (launch_k in mg_kernels.h): the next kernel may be
+// scheduled while this one drains. pdl_enter() at the top of a kernel first waits until
+// the preceding kernel has completed and its writes are visible (griddepcontrol.wait;
+// a no-op without a programmatic dependency), so no data hazard is relaxed, then lets the
+// following kernel start launching (griddepcontrol.launch_dependents).
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+#ifdef JMG_PDL_EARLY_TRIGGER
+  asm volatile("griddepcontrol.launch_dependents;\n" :::);
+#endif
+}
+
 template <typename T>
 struct LvlTable {
   Lvl<T> l[kMaxLevels];

@@ -153,10 +153,11 @@ int validate_and_layout(JmgPlan* p) {
   p->off_tab32 = take(sizeof(LvlTable<float>));
   p->fcg = p->cfg.outer == JMG_OUTER_FCG;
   if (p->fcg) {
-    const size_t b8 = p->lv[0].elems * 8;
-    p->off_rho = take(b8);
-    p->off_d = take(b8);
-    p->off_q = take(b8);
+    // FP64 cycles: FP64 rho, d, q, z; mixed: FP32 d, q (x and the true residual are FP64)
+    const size_t b8 = p->lv[0].elems * 8, bv = p->lv[0].elems * (p->mixed ? 4 : 8);
+    p->off_rho = p->mixed ? 0 : take(b8);
+    p->off_d = take(bv);
+    p->off_q = take(bv);
     p->off_z64 = p->mixed ? 0 : take(b8);
     p->off_fcg_parts = take((size_t)fcg_num_parts() * 5 * 8);
     p->off_tab64z = take(sizeof(LvlTable<double>));
@@ -376,9 +377,6 @@ void emit_fcg_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaSt
   CycleParams cp = cycle_params(p, p->off_diag);
   double* fp = ptr<double>(ws, p->off_fcg_parts);
   const int np = fcg_num_parts();
-  double* rho = ptr<double>(ws, p->off_rho);
-  double* d = ptr<double>(ws, p->off_d);
-  double* q = ptr<double>(ws, p->off_q);
   const int inner = p->cfg.inner_cycles > 0 ? p->cfg.inner_cycles : 1;
   // the first sweep may start from a zero guess without reading phi when level 0 runs its
   // own sweeps; otherwise the correction is zeroed first
@@ -392,11 +390,12 @@ void emit_fcg_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaSt
       emit_cycle<float>(p, t32, ptr<LvlTable<float>>(ws, p->off_tab32), cp, 0, p->cfg.fcycle != 0, false, s,
                         nullptr, &top);
     }
-    launch_fcg_iter<float>(p->dim, l0, t32.l[0].phi, d, q, rho, t32.l[0].rhs, fp, fp + 2 * np, fp + 4 * np, s);
+    launch_fcg32_iter(p->dim, l0, t32.l[0], t32.l[0].phi, ptr<float>(ws, p->off_d), ptr<float>(ws, p->off_q),
+                      t32.l[0].rhs, fp, fp + 2 * np, fp + 4 * np, s);
   } else {
     LvlTable<double> tz = make_table<double>(p, ws);
     tz.l[0].phi = ptr<double>(ws, p->off_z64);
-    tz.l[0].rhs = rho;
+    tz.l[0].rhs = ptr<double>(ws, p->off_rho);
     if (!zero_first) cudaMemsetAsync(tz.l[0].phi, 0, p->lv[0].elems * 8, s);
     for (int k = 0; k < inner; ++k) {
       EmitTop top;
@@ -404,7 +403,8 @@ void emit_fcg_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaSt
       emit_cycle<double>(p, tz, ptr<LvlTable<double>>(ws, p->off_tab64z), cp, 0, p->cfg.fcycle != 0, false, s,
                          nullptr, &top);
     }
-    launch_fcg_iter<double>(p->dim, l0, tz.l[0].phi, d, q, rho, nullptr, fp, fp + 2 * np, fp + 4 * np, s);
+    launch_fcg_iter<double>(p->dim, l0, tz.l[0].phi, ptr<double>(ws, p->off_d), ptr<double>(ws, p->off_q),
+                            ptr<double>(ws, p->off_rho), nullptr, fp, fp + 2 * np, fp + 4 * np, s);
   }
   launch_loop_step(st, fp + 4 * np, np, loop_mode(p), p->cfg.epsilon, p->cfg.rtol, p->cfg.max_iters_outer, handle,
                    s);
@@ -469,8 +469,11 @@ void emit_prologue(const JmgPlan* p, void* ws, unsigned long long handle, cudaSt
   int nparts = p->nparts;
   if (p->fcg) {
     double* fp = ptr<double>(ws, p->off_fcg_parts);
-    launch_fcg_init(p->dim, l0, ptr<double>(ws, p->off_rho), ptr<double>(ws, p->off_d), ptr<double>(ws, p->off_q),
-                    p->mixed ? lvl32(p, ws, 0).rhs : nullptr, fp, s);
+    if (p->mixed)
+      launch_fcg32_init(p->dim, l0, lvl32(p, ws, 0).rhs, ptr<float>(ws, p->off_d), ptr<float>(ws, p->off_q), fp, s);
+    else
+      launch_fcg_init(p->dim, l0, ptr<double>(ws, p->off_rho), ptr<double>(ws, p->off_d), ptr<double>(ws, p->off_q),
+                      nullptr, fp, s);
     launch_loop_init(st, fp, fcg_num_parts(), mode, p->cfg.rtol, p->cfg.max_iters_outer, handle, s);
     return;
   }
@@ -500,7 +503,7 @@ long long body_launches(const JmgPlan* p) {
       memset(&t, 0, sizeof(t));
       for (int k = 0; k < inner; ++k) emit_cycle<double>(p, t, nullptr, cp, 0, p->cfg.fcycle != 0, false, nullptr, &n);
     }
-    return n + 3 + 1 + (zero_first ? 0 : 1);  // FCG update, loop step (+ memset node)
+    return n + (p->mixed ? 4 : 3) + 1 + (zero_first ? 0 : 1);  // FCG update, loop step (+ memset node)
   }
   if (!p->mixed) {
     LvlTable<double> t;
@@ -665,6 +668,15 @@ __global__ void k_write_i64(long long* out, long long v) { *out = v; }
 
 int jmg::set_error_message(int code, const char* msg) { return set_err(code, "%s", msg); }
 
+// JMG_PDL=0 turns programmatic dependent launch off (read once per process)
+bool jmg::pdl_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("JMG_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 // ---------------------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------------------
@@ -746,10 +758,10 @@ int jmg_solve(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs
   launch_store_table<double>(make_table<double>(p, ws), ptr<LvlTable<double>>(ws, p->off_tab64), s);
   if (p->fcg) {
     // zero frames of the FCG vectors (their kernels write interiors only)
-    const size_t b8 = p->lv[0].elems * 8;
-    JMG_CUDA(cudaMemsetAsync(ptr<char>(ws, p->off_rho), 0, b8, s));
-    JMG_CUDA(cudaMemsetAsync(ptr<char>(ws, p->off_d), 0, b8, s));
-    JMG_CUDA(cudaMemsetAsync(ptr<char>(ws, p->off_q), 0, b8, s));
+    const size_t b8 = p->lv[0].elems * 8, bv = p->lv[0].elems * (p->mixed ? 4 : 8);
+    if (!p->mixed) JMG_CUDA(cudaMemsetAsync(ptr<char>(ws, p->off_rho), 0, b8, s));
+    JMG_CUDA(cudaMemsetAsync(ptr<char>(ws, p->off_d), 0, bv, s));
+    JMG_CUDA(cudaMemsetAsync(ptr<char>(ws, p->off_q), 0, bv, s));
     if (!p->mixed) {
       JMG_CUDA(cudaMemsetAsync(ptr<char>(ws, p->off_z64), 0, b8, s));
       LvlTable<double> tz = make_table<double>(p, ws);

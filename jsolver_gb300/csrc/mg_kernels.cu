@@ -26,6 +26,7 @@ namespace jmg {
 // (one sub-lattice), and four passes make a sweep (solver_2d.py:684).
 template <typename T>
 __global__ void k_sweep_color2d(Lvl<T> a, int color, int zero_other, int row_par) {
+  pdl_enter();
   const int r = blockIdx.y * blockDim.y + threadIdx.y;
   const int i = row_par < 0 ? r + 2 : 2 + row_par + 2 * r;
   if (i > a.my) return;
@@ -39,6 +40,7 @@ __global__ void k_sweep_color2d(Lvl<T> a, int color, int zero_other, int row_par
 // 3D: blockDim (64, 4, 1); grid z walks planes.
 template <typename T>
 __global__ void k_sweep_color3d(Lvl<T> a, int color, int zero_other) {
+  pdl_enter();
   const int k = blockIdx.z + 2;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
   if (j > a.my || k > a.mz) return;
@@ -54,6 +56,7 @@ __global__ void k_sweep_color3d(Lvl<T> a, int color, int zero_other) {
 // Over the full padded coarse array: phi_c = 0, rhs_c = restricted defect inside, 0 on the frame.
 template <typename T>
 __global__ void k_restrict2d(Lvl<T> f, Lvl<T> c) {
+  pdl_enter();
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
   if (I > c.mx + 2 || J > c.my + 2) return;
@@ -66,6 +69,7 @@ __global__ void k_restrict2d(Lvl<T> f, Lvl<T> c) {
 
 template <typename T>
 __global__ void k_restrict3d(Lvl<T> f, Lvl<T> c) {
+  pdl_enter();
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
   const int K = blockIdx.z;
@@ -79,6 +83,7 @@ __global__ void k_restrict3d(Lvl<T> f, Lvl<T> c) {
 
 template <typename T>
 __global__ void k_prolong2d(Lvl<T> f, Lvl<T> c, int diag) {
+  pdl_enter();
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
   if (i > f.my || j > f.mx) return;
@@ -91,6 +96,7 @@ __global__ void k_prolong2d(Lvl<T> f, Lvl<T> c, int diag) {
 
 template <typename T>
 __global__ void k_prolong3d(Lvl<T> f, Lvl<T> c, int bilinear) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
   const int k = blockIdx.z + 2;
@@ -246,6 +252,7 @@ __device__ void blk_cycle(const LvlTable<T>* __restrict__ tab, const CycleParams
 template <typename T, int DIM>
 __global__ void __launch_bounds__(1024) k_coarse_cycle(const LvlTable<T>* tab, CycleParams cp, int lev, int fcycle,
                                                       int skip_pre) {
+  pdl_enter();
   blk_cycle<T, DIM>(tab, cp, lev, fcycle != 0, skip_pre != 0);
 }
 
@@ -275,7 +282,7 @@ void launch_sweep(int dim, Lvl<T>& a, cudaStream_t s, bool zero_init) {
     const int colour[4] = {0, 0, 1, 1}, rpar[4] = {1, 0, 0, 1};
     for (int q = 0; q < 4; ++q) {
       dim3 b(64, 4), g(cdiv(a.mx / 2, 64), cdiv((a.my - 1 + 1) / 2, 4));
-      k_sweep_color2d<T><<<g, b, 0, s>>>(a, colour[q], 0, rpar[q]);
+      launch_k(k_sweep_color2d<T>, g, b, 0, s, a, colour[q], 0, rpar[q]);
     }
     return;
   }
@@ -283,10 +290,10 @@ void launch_sweep(int dim, Lvl<T>& a, cudaStream_t s, bool zero_init) {
     const int zero = (zero_init && color == 0) ? 1 : 0;
     if (dim == 2) {
       dim3 b(64, 4), g(cdiv(a.mx / 2, 64), cdiv(a.my - 1, 4));
-      k_sweep_color2d<T><<<g, b, 0, s>>>(a, color, zero, -1);
+      launch_k(k_sweep_color2d<T>, g, b, 0, s, a, color, zero, -1);
     } else {
       dim3 b(64, 4, 1), g(cdiv(a.mx / 2, 64), cdiv(a.my - 1, 4), a.mz - 1);
-      k_sweep_color3d<T><<<g, b, 0, s>>>(a, color, zero);
+      launch_k(k_sweep_color3d<T>, g, b, 0, s, a, color, zero);
     }
   }
 }
@@ -297,10 +304,10 @@ void launch_restrict(int dim, const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s) 
     launch_restrict_tile2d<T>(f, c, s);
   } else if (dim == 2) {
     dim3 b(32, 8), g(cdiv(c.mx + 3, 32), cdiv(c.my + 3, 8));
-    k_restrict2d<T><<<g, b, 0, s>>>(f, c);
+    launch_k(k_restrict2d<T>, g, b, 0, s, f, c);
   } else {
     dim3 b(32, 8, 1), g(cdiv(c.mx + 3, 32), cdiv(c.my + 3, 8), c.mz + 3);
-    k_restrict3d<T><<<g, b, 0, s>>>(f, c);
+    launch_k(k_restrict3d<T>, g, b, 0, s, f, c);
   }
 }
 
@@ -308,10 +315,10 @@ template <typename T>
 void launch_prolong(int dim, const Lvl<T>& f, const Lvl<T>& c, int diag, cudaStream_t s) {
   if (dim == 2) {
     dim3 b(64, 4), g(cdiv(f.mx - 1, 64), cdiv(f.my - 1, 4));
-    k_prolong2d<T><<<g, b, 0, s>>>(f, c, diag);
+    launch_k(k_prolong2d<T>, g, b, 0, s, f, c, diag);
   } else {
     dim3 b(64, 4, 1), g(cdiv(f.mx - 1, 64), cdiv(f.my - 1, 4), f.mz - 1);
-    k_prolong3d<T><<<g, b, 0, s>>>(f, c, diag);
+    launch_k(k_prolong3d<T>, g, b, 0, s, f, c, diag);
   }
 }
 
@@ -319,9 +326,9 @@ template <typename T>
 void launch_coarse_cycle(int dim, const LvlTable<T>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
                          cudaStream_t s) {
   if (dim == 2)
-    k_coarse_cycle<T, 2><<<1, 1024, 0, s>>>(tab, cp, lev, fcycle, skip_pre);
+    launch_k(k_coarse_cycle<T, 2>, dim3(1), dim3(1024), 0, s, tab, cp, lev, fcycle, skip_pre);
   else
-    k_coarse_cycle<T, 3><<<1, 1024, 0, s>>>(tab, cp, lev, fcycle, skip_pre);
+    launch_k(k_coarse_cycle<T, 3>, dim3(1), dim3(1024), 0, s, tab, cp, lev, fcycle, skip_pre);
 }
 
 template <typename T>

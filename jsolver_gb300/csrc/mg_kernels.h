@@ -7,6 +7,24 @@
 
 namespace jmg {
 
+// Kernel launch with programmatic stream serialisation (PDL) unless JMG_PDL=0. The
+// kernel must call pdl_enter() before touching memory (mg_common.cuh).
+bool pdl_enabled();
+template <typename... KArgs, typename... Args>
+inline void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 struct CycleParams {
   int last_level;  // L-2: the deepest level visited (solver_2d.py:601)
   int nu1, nu2, gamma;
@@ -105,6 +123,11 @@ int fcg_num_parts();
 // rho = rhs - L x (x = a.phi), d = q = 0, r32 = float(rho) (nullable); partials of rho^2
 void launch_fcg_init(int dim, const Lvl<double>& a, double* rho, double* d, double* q, float* r32, double* parts,
                      cudaStream_t s);
+// mixed precision (FP32 directions d, q; FP64 x and true residual): init and one step
+// (dots, directions, x update, residual: 4 launches)
+void launch_fcg32_init(int dim, const Lvl<double>& a, float* r32, float* d, float* q, double* parts, cudaStream_t s);
+void launch_fcg32_iter(int dim, const Lvl<double>& a, const Lvl<float>& a32, const float* z, float* d, float* q,
+                       float* r32, double* parts_dots, double* parts_dir, double* parts_res, cudaStream_t s);
 // one FCG step after the preconditioner produced z: dots, direction, update (3 launches)
 template <typename TZ>
 void launch_fcg_iter(int dim, const Lvl<double>& a, const TZ* z, double* d, double* q, double* rho, float* r32,

@@ -115,6 +115,7 @@ __device__ __forceinline__ double apply_L(const Lvl<double>& a, const TZ* z, lon
 template <int DIM>
 __global__ void __launch_bounds__(kThreads) k_fcg_init(Lvl<double> a, double* rho, double* d, double* q, float* r32,
                                                       double* parts) {
+  pdl_enter();
   double s = 0.0, unused = 0.0;
   JMG_FOR_POINTS(a, p) {
     const double r = DIM == 2 ? defect_point2d<double>(a, a.phi, p)
@@ -133,6 +134,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_init(Lvl<double> a, double* rh
 template <int DIM, typename TZ>
 __global__ void __launch_bounds__(kThreads) k_fcg_dots(Lvl<double> a, const TZ* z, const double* d, const double* q,
                                                       double* parts) {
+  pdl_enter();
   double zq = 0.0, dq = 0.0;
   JMG_FOR_POINTS(a, p) {
     const double qp = q[p];
@@ -150,6 +152,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_dots(Lvl<double> a, const TZ* 
 template <int DIM, typename TZ>
 __global__ void __launch_bounds__(kThreads) k_fcg_dir(Lvl<double> a, const TZ* z, double* d, double* q,
                                                      const double* rho, const double* parts_in, double* parts) {
+  pdl_enter();
   double zq, dq;
   totals2(parts_in, &zq, &dq);
   const double beta = dq != 0.0 ? zq / dq : 0.0;
@@ -173,6 +176,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_dir(Lvl<double> a, const TZ* z
 template <int DIM>
 __global__ void __launch_bounds__(kThreads) k_fcg_step(Lvl<double> a, const double* d, const double* q, double* rho,
                                                       float* r32, const double* parts_in, double* parts) {
+  pdl_enter();
   double dr, dq;
   totals2(parts_in, &dr, &dq);
   const double alpha = dq != 0.0 ? dr / dq : 0.0;
@@ -188,27 +192,155 @@ __global__ void __launch_bounds__(kThreads) k_fcg_step(Lvl<double> a, const doub
   if (threadIdx.x == 0) parts[blockIdx.x] = s;
 }
 
+// ---- mixed precision: FP32 directions, FP64 solution and true residual ----------------
+// Inside FP64 refinement the search directions need only the preconditioner's accuracy:
+// d and q = L d are kept in FP32 and built with the FP32 coefficient mirrors, the step
+// x += alpha d is FP64, and the residual is recomputed exactly, rho = rhs - L x in FP64,
+// every step (so the stopping test reads the true residual; no recurrence to drift).
+
+// L z in FP32 with the FP32 coefficients (9-point terms when present)
+template <int DIM>
+__device__ __forceinline__ float apply_L32(const Lvl<float>& a, const float* z, long long p) {
+  float t = a.acc[p] * z[p];
+  t = fmaf(-a.wx[p - 1], z[p - 1], t);
+  t = fmaf(-a.wx[p], z[p + 1], t);
+  t = fmaf(-a.wy[p - a.P], z[p - a.P], t);
+  t = fmaf(-a.wy[p], z[p + a.P], t);
+  if (DIM == 3) {
+    t = fmaf(-a.wz[p - a.S], z[p - a.S], t);
+    t = fmaf(-a.wz[p], z[p + a.S], t);
+  }
+  if (DIM == 2 && a.xll) {
+    const int P = a.P;
+    float o = a.xll[p] * z[p - P - 1];
+    o = fmaf(a.xrl[p], z[p - P + 1], o);
+    o = fmaf(a.xlr[p], z[p + P - 1], o);
+    o = fmaf(a.xrr[p], z[p + P + 1], o);
+    t = t - o;
+  }
+  return -t;
+}
+
+// rho = rhs - L x (FP64), r32 = float(rho), d32 = q32 = 0; partials of rho . rho
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) k_fcg32_init(Lvl<double> a, float* r32, float* d, float* q,
+                                                        double* parts) {
+  pdl_enter();
+  double s = 0.0, unused = 0.0;
+  JMG_FOR_POINTS(a, p) {
+    const double r = DIM == 2 ? defect_point2d<double>(a, a.phi, p)
+                              : defect_point3d<double>(a.phi, a.rhs, a.wx, a.wy, a.wz, a.acc, p, a.P, a.S);
+    r32[p] = (float)r;
+    if (d) {
+      d[p] = 0.f;
+      q[p] = 0.f;
+    }
+    s = fma(r, r, s);
+  }
+  block_sum2(s, unused);
+  if (threadIdx.x == 0) parts[blockIdx.x] = s;
+}
+
+// partials of z . q and d . q (FP32 products, FP64 block sums)
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) k_fcg32_dots(Lvl<double> a, const float* z, const float* d, const float* q,
+                                                        double* parts) {
+  pdl_enter();
+  float zq = 0.f, dq = 0.f;
+  JMG_FOR_POINTS(a, p) {
+    const float qp = q[p];
+    zq = fmaf(z[p], qp, zq);
+    dq = fmaf(d[p], qp, dq);
+  }
+  double a0 = zq, a1 = dq;
+  block_sum2(a0, a1);
+  if (threadIdx.x == 0) {
+    parts[2 * blockIdx.x] = a0;
+    parts[2 * blockIdx.x + 1] = a1;
+  }
+}
+
+// beta; d <- z - beta d, q <- L32 z - beta q (FP32); partials of d . r32 and d . q
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) k_fcg32_dir(Lvl<double> a, Lvl<float> a32, const float* z, float* d,
+                                                       float* q, const float* r32, const double* parts_in,
+                                                       double* parts) {
+  pdl_enter();
+  double zq, dq;
+  totals2(parts_in, &zq, &dq);
+  const float beta = dq != 0.0 ? (float)(zq / dq) : 0.f;
+  float dr = 0.f, dqn = 0.f;
+  JMG_FOR_POINTS(a, p) {
+    const float dn = fmaf(-beta, d[p], z[p]);
+    const float qn = fmaf(-beta, q[p], apply_L32<DIM>(a32, z, p));
+    d[p] = dn;
+    q[p] = qn;
+    dr = fmaf(dn, r32[p], dr);
+    dqn = fmaf(dn, qn, dqn);
+  }
+  double b0 = dr, b1 = dqn;
+  block_sum2(b0, b1);
+  if (threadIdx.x == 0) {
+    parts[2 * blockIdx.x] = b0;
+    parts[2 * blockIdx.x + 1] = b1;
+  }
+}
+
+// alpha; x += alpha d (FP64)
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) k_fcg32_x(Lvl<double> a, const float* d, const double* parts_in) {
+  pdl_enter();
+  double dr, dq;
+  totals2(parts_in, &dr, &dq);
+  const double alpha = dq != 0.0 ? dr / dq : 0.0;
+  JMG_FOR_POINTS(a, p) a.phi[p] = fma(alpha, (double)d[p], a.phi[p]);
+}
+
 }  // namespace
 
 int fcg_num_parts() { return kBlocks; }
 
+void launch_fcg32_init(int dim, const Lvl<double>& a, float* r32, float* d, float* q, double* parts,
+                       cudaStream_t s) {
+  if (dim == 2) launch_k(k_fcg32_init<2>, dim3(kBlocks), dim3(kThreads), 0, s, a, r32, d, q, parts);
+  else launch_k(k_fcg32_init<3>, dim3(kBlocks), dim3(kThreads), 0, s, a, r32, d, q, parts);
+}
+
+// one step after the cycle produced z (FP32): dots, directions, x update, true residual
+void launch_fcg32_iter(int dim, const Lvl<double>& a, const Lvl<float>& a32, const float* z, float* d, float* q,
+                       float* r32, double* parts_dots, double* parts_dir, double* parts_res, cudaStream_t s) {
+  if (dim == 2) {
+    launch_k(k_fcg32_dots<2>, dim3(kBlocks), dim3(kThreads), 0, s, a, z, d, q, parts_dots);
+    launch_k(k_fcg32_dir<2>, dim3(kBlocks), dim3(kThreads), 0, s, a, a32, z, d, q, r32, parts_dots, parts_dir);
+    launch_k(k_fcg32_x<2>, dim3(kBlocks), dim3(kThreads), 0, s, a, d, parts_dir);
+    launch_k(k_fcg32_init<2>, dim3(kBlocks), dim3(kThreads), 0, s, a, r32, (float*)nullptr, (float*)nullptr,
+             parts_res);
+  } else {
+    launch_k(k_fcg32_dots<3>, dim3(kBlocks), dim3(kThreads), 0, s, a, z, d, q, parts_dots);
+    launch_k(k_fcg32_dir<3>, dim3(kBlocks), dim3(kThreads), 0, s, a, a32, z, d, q, r32, parts_dots, parts_dir);
+    launch_k(k_fcg32_x<3>, dim3(kBlocks), dim3(kThreads), 0, s, a, d, parts_dir);
+    launch_k(k_fcg32_init<3>, dim3(kBlocks), dim3(kThreads), 0, s, a, r32, (float*)nullptr, (float*)nullptr,
+             parts_res);
+  }
+}
+
 void launch_fcg_init(int dim, const Lvl<double>& a, double* rho, double* d, double* q, float* r32, double* parts,
                      cudaStream_t s) {
-  if (dim == 2) k_fcg_init<2><<<kBlocks, kThreads, 0, s>>>(a, rho, d, q, r32, parts);
-  else k_fcg_init<3><<<kBlocks, kThreads, 0, s>>>(a, rho, d, q, r32, parts);
+  if (dim == 2) launch_k(k_fcg_init<2>, dim3(kBlocks), dim3(kThreads), 0, s, a, rho, d, q, r32, parts);
+  else launch_k(k_fcg_init<3>, dim3(kBlocks), dim3(kThreads), 0, s, a, rho, d, q, r32, parts);
 }
 
 template <typename TZ>
 void launch_fcg_iter(int dim, const Lvl<double>& a, const TZ* z, double* d, double* q, double* rho, float* r32,
                      double* parts_dots, double* parts_dir, double* parts_res, cudaStream_t s) {
   if (dim == 2) {
-    k_fcg_dots<2, TZ><<<kBlocks, kThreads, 0, s>>>(a, z, d, q, parts_dots);
-    k_fcg_dir<2, TZ><<<kBlocks, kThreads, 0, s>>>(a, z, d, q, rho, parts_dots, parts_dir);
-    k_fcg_step<2><<<kBlocks, kThreads, 0, s>>>(a, d, q, rho, r32, parts_dir, parts_res);
+    launch_k(k_fcg_dots<2, TZ>, dim3(kBlocks), dim3(kThreads), 0, s, a, z, d, q, parts_dots);
+    launch_k(k_fcg_dir<2, TZ>, dim3(kBlocks), dim3(kThreads), 0, s, a, z, d, q, rho, parts_dots, parts_dir);
+    launch_k(k_fcg_step<2>, dim3(kBlocks), dim3(kThreads), 0, s, a, d, q, rho, r32, parts_dir, parts_res);
   } else {
-    k_fcg_dots<3, TZ><<<kBlocks, kThreads, 0, s>>>(a, z, d, q, parts_dots);
-    k_fcg_dir<3, TZ><<<kBlocks, kThreads, 0, s>>>(a, z, d, q, rho, parts_dots, parts_dir);
-    k_fcg_step<3><<<kBlocks, kThreads, 0, s>>>(a, d, q, rho, r32, parts_dir, parts_res);
+    launch_k(k_fcg_dots<3, TZ>, dim3(kBlocks), dim3(kThreads), 0, s, a, z, d, q, parts_dots);
+    launch_k(k_fcg_dir<3, TZ>, dim3(kBlocks), dim3(kThreads), 0, s, a, z, d, q, rho, parts_dots, parts_dir);
+    launch_k(k_fcg_step<3>, dim3(kBlocks), dim3(kThreads), 0, s, a, d, q, rho, r32, parts_dir, parts_res);
   }
 }
 

@@ -18,6 +18,7 @@ int residual_f32_parts2d(int mx, int my) { return ((mx - 1 + kRX - 1) / kRX) * (
 
 __global__ void __launch_bounds__(256) k_residual_f32_2d(Lvl<double> a, float* __restrict__ r32,
                                                          double* __restrict__ parts) {
+  pdl_enter();
   __shared__ double Phi[kRY + 2][kRX + 2];  // rows i0-1 .. i0+RY, columns j0-1 .. j0+RX
   __shared__ double red[8];
   const int i0 = 2 + blockIdx.y * kRY, j0 = 2 + blockIdx.x * kRX;
@@ -61,7 +62,7 @@ __global__ void __launch_bounds__(256) k_residual_f32_2d(Lvl<double> a, float* _
 
 void launch_residual_f32_2d(const Lvl<double>& a, float* r32, double* parts, cudaStream_t s) {
   dim3 b(32, 8), g((unsigned)((a.mx - 1 + kRX - 1) / kRX), (unsigned)((a.my - 1 + kRY - 1) / kRY));
-  k_residual_f32_2d<<<g, b, 0, s>>>(a, r32, parts);
+  launch_k(k_residual_f32_2d, g, b, 0, s, a, r32, parts);
 }
 
 
@@ -81,6 +82,7 @@ constexpr int kFR = kDR + 2, kFC = kDC + 2;                  // with the one-poi
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_restrict_tile2d(Lvl<T> f, Lvl<T> c) {
+  pdl_enter();
   __shared__ T Phi[kFR][kFC];
   __shared__ T Def[kDR][kDC];
   const int J0 = blockIdx.y * kCJ, I0 = blockIdx.x * kCI;
@@ -131,7 +133,7 @@ __global__ void __launch_bounds__(256) k_restrict_tile2d(Lvl<T> f, Lvl<T> c) {
 template <typename T>
 void launch_restrict_tile2d(const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s) {
   dim3 g((unsigned)((c.mx + 3 + kCI - 1) / kCI), (unsigned)((c.my + 3 + kCJ - 1) / kCJ));
-  k_restrict_tile2d<T><<<g, 256, 0, s>>>(f, c);
+  launch_k(k_restrict_tile2d<T>, g, dim3(256), 0, s, f, c);
 }
 
 template void launch_restrict_tile2d<double>(const Lvl<double>&, const Lvl<double>&, cudaStream_t);
