@@ -343,24 +343,26 @@ def main():
             solve_dev(stream)
         err_exact = (float(np.abs(out.cpu().numpy() - p["phi_exact"]).max()) if "phi_exact" in p else None)
 
-        # dominant kernel: the fine-level FP64 red-black sweep (two colour launches), timed
-        # alone with CUDA events on its stream, L2 flushed before every sweep
+        # the fine-level red-black sweep of the form's cycles (FP64, or FP32 in the mixed
+        # forms; two colour launches), timed alone with CUDA events on its stream, L2
+        # flushed before every sweep
         nsw = 20
-        _lib.check(lib.jmg_op_smooth_ws(plan.handle, 0, 3, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()),
-                                        vp(stream.cuda_stream)))
+        smooth = lib.jmg_op_smooth32_ws if precision == "mixed" else lib.jmg_op_smooth_ws
+        elem = 4 if precision == "mixed" else 8
+        _lib.check(smooth(plan.handle, 0, 3, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()), vp(stream.cuda_stream)))
         sw = []
         for _ in range(nsw):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            _lib.check(lib.jmg_op_smooth_ws(plan.handle, 0, 1, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()),
-                                            vp(stream.cuda_stream)))
+            _lib.check(smooth(plan.handle, 0, 1, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()),
+                              vp(stream.cuda_stream)))
             e1.record(stream)
             sw.append((e0, e1))
         stream.synchronize()
         sweep_ms = float(np.mean([a.elapsed_time(b) for a, b in sw]))
         n0 = (m + 3) ** dim
-        alg_bytes_sweep = (dim + 4) * 8 * n0  # (d+4)*s*N0: phi, rhs, d faces, 1/A_cc read; phi written
+        alg_bytes_sweep = (dim + 4) * elem * n0  # (d+4)*s*N0: phi, rhs, d faces, 1/A_cc read; phi written
         launch_ms = sweep_ms / 2
         achieved = alg_bytes_sweep / (sweep_ms * 1e-3) / 1e9
 
@@ -411,7 +413,7 @@ def main():
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get(f"sweep_fp64_{dim}d_{m}")
+            traffic = json.load(f).get(f"sweep_{'fp32' if elem == 4 else 'fp64'}_{dim}d_{m}")
     except (OSError, ValueError):
         pass
 
@@ -432,7 +434,9 @@ def main():
         "speedup_vs_plain_fp64": (plain["ms"] / ms) if plain else None,
         "guess_rel_residual": guess_rel_res,
         "max_err_vs_exact_discrete": err_exact,
-        "roofline": {"bound": "hbm", "kernel": f"k_sweep_color{dim}d<double> (fine level; 2 launches per sweep)",
+        "roofline": {"bound": "hbm",
+                     "kernel": f"k_sweep_color{dim}d<{'float' if elem == 4 else 'double'}> (fine level; 2 launches "
+                               "per sweep)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src, "alg_bytes_per_sweep": alg_bytes_sweep,
                      "alg_bytes_per_launch": alg_bytes_sweep / 2, "launch_ms": launch_ms, "traffic": traffic},

@@ -173,6 +173,10 @@ int jmg_solve_fixed_vjp(JmgPlan* plan, const double* phi0, const double* rhs, co
  * red_black_gauss_seidel (solver_2d.py:670-692) without copies, for timing it alone. */
 int jmg_op_smooth_ws(JmgPlan* plan, int level, int nsweeps, void* workspace, size_t workspace_bytes,
                      jmg_stream_t stream);
+/* The same for the FP32 arrays of a mixed-precision plan (the smoother of its FP32
+ * cycles), for timing it alone. */
+int jmg_op_smooth32_ws(JmgPlan* plan, int level, int nsweeps, void* workspace, size_t workspace_bytes,
+                       jmg_stream_t stream);
 
 /* Kernel launches of one jmg_solve: the fixed part (copies, hierarchy, loop set-up) and
  * the part repeated per loop iteration (one cycle plus its stopping test). No reference

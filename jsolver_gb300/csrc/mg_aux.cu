@@ -119,10 +119,12 @@ void launch_distance_snapshot(const Box& b, double* old_phi, const double* phi, 
 // residual norms (deterministic)
 // ------------------------------------------------------------------------------------
 
-constexpr int kResBlocks = 304;  // 2 x 152 SMs, fixed so the reduction order is fixed
+// 304 blocks (2 per SM) up to 4096 interior rows, 1216 (8 per SM) above: fixed per
+// problem size, so the reduction order, and the result, is reproducible
+inline int res_blocks(const Box& b) { return (b.ny - 3) * (b.nz > 1 ? b.nz - 3 : 1) > 4096 ? 1216 : 304; }
 constexpr int kResThreads = 256;
 
-int residual_num_parts(int, const Box&) { return kResBlocks; }
+int residual_num_parts(int, const Box& b) { return res_blocks(b); }
 
 __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -170,12 +172,12 @@ __global__ void k_residual_partials(Lvl<T> a, const T* phi, double* parts, float
 }
 
 template <typename T>
-void launch_residual_partials(int dim, const Lvl<T>& a, const T* phi_or_null, double* parts, int, cudaStream_t s,
+void launch_residual_partials(int dim, const Lvl<T>& a, const T* phi_or_null, double* parts, int nparts, cudaStream_t s,
                               float* r32) {
   if (dim == 2)
-    launch_k(k_residual_partials<T, 2>, dim3(kResBlocks), dim3(kResThreads), 0, s, a, phi_or_null, parts, r32);
+    launch_k(k_residual_partials<T, 2>, dim3(nparts), dim3(kResThreads), 0, s, a, phi_or_null, parts, r32);
   else
-    launch_k(k_residual_partials<T, 3>, dim3(kResBlocks), dim3(kResThreads), 0, s, a, phi_or_null, parts, r32);
+    launch_k(k_residual_partials<T, 3>, dim3(nparts), dim3(kResThreads), 0, s, a, phi_or_null, parts, r32);
 }
 template void launch_residual_partials<double>(int, const Lvl<double>&, const double*, double*, int, cudaStream_t,
                                                float*);

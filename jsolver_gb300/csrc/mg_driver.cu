@@ -220,6 +220,19 @@ int jmg::coarse_setup(JmgPlan* p) {
       break;
     }
   }
+  p->coarse_smem32 = 0;
+  const char* c32 = getenv("JMG_COARSE32");
+  // opt-in (JMG_COARSE32=smem): staging ~150 KB per launch costs more than the L2 round
+  // trips it saves (2D 1024^2 mixed + FCG: 10.87 ms with it, 10.32 ms without)
+  if (p->mixed && dim == 2 && !p->off_diag && !p->cluster_ranks && c32 && std::strcmp(c32, "smem") == 0) {
+    int mx[kMaxLevels], my[kMaxLevels];
+    for (int l = 0; l < p->used && l < kMaxLevels; ++l) {
+      mx[l] = p->lv[l].m[0];
+      my[l] = p->lv[l].m[1];
+    }
+    const size_t b = coarse_smem32_bytes(mx, my, p->coarse_start, last);
+    if (b <= 200 * 1024 && prepare_coarse_smem32(b) == 0) p->coarse_smem32 = b;
+  }
   cudaGetLastError();  // a refused attribute or occupancy query leaves no sticky error
   p->coarse_ready = true;
   return JMG_OK;
@@ -331,6 +344,9 @@ void emit_cycle(const JmgPlan* p, LvlTable<T>& tab, const LvlTable<T>* dtab, con
     else if (p->cluster_ranks)
       launch_coarse_cluster<T>(dim, dtab, p->cluster, cp, fcycle ? 1 : 0, skip_pre ? 1 : 0,
                                sizeof(T) == 8 ? p->cluster_smem64 : p->cluster_smem32, s);
+    else if (sizeof(T) == 4 && p->coarse_smem32)
+      launch_coarse_smem32(reinterpret_cast<const LvlTable<float>*>(dtab), cp, lev, fcycle ? 1 : 0,
+                           skip_pre ? 1 : 0, p->coarse_smem32, s);
     else launch_coarse_cycle<T>(dim, dtab, cp, lev, fcycle ? 1 : 0, skip_pre ? 1 : 0, s);
     return;
   }
@@ -406,8 +422,8 @@ void emit_fcg_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaSt
     launch_fcg_iter<double>(p->dim, l0, tz.l[0].phi, ptr<double>(ws, p->off_d), ptr<double>(ws, p->off_q),
                             ptr<double>(ws, p->off_rho), nullptr, fp, fp + 2 * np, fp + 4 * np, s);
   }
-  launch_loop_step(st, fp + 4 * np, np, loop_mode(p), p->cfg.epsilon, p->cfg.rtol, p->cfg.max_iters_outer, handle,
-                   s);
+  launch_loop_step(st, fp + 4 * np, fcg_parts_used(p->dim, l0), loop_mode(p), p->cfg.epsilon, p->cfg.rtol,
+                   p->cfg.max_iters_outer, handle, s);
 }
 
 // body of one loop iteration (captured into the WHILE node's body graph)
@@ -474,7 +490,7 @@ void emit_prologue(const JmgPlan* p, void* ws, unsigned long long handle, cudaSt
     else
       launch_fcg_init(p->dim, l0, ptr<double>(ws, p->off_rho), ptr<double>(ws, p->off_d), ptr<double>(ws, p->off_q),
                       nullptr, fp, s);
-    launch_loop_init(st, fp, fcg_num_parts(), mode, p->cfg.rtol, p->cfg.max_iters_outer, handle, s);
+    launch_loop_init(st, fp, fcg_parts_used(p->dim, l0), mode, p->cfg.rtol, p->cfg.max_iters_outer, handle, s);
     return;
   }
   if (mixed_fused(p)) {
@@ -971,6 +987,16 @@ int jmg_op_smooth_ws(JmgPlan* p, int level, int nsweeps, void* ws, size_t bytes,
   if (rc || (rc = level_check(p, level, false))) return rc;
   Lvl<double> a = lvl64(p, ws, level);
   for (int k = 0; k < nsweeps; ++k) launch_sweep<double>(p->dim, a, (cudaStream_t)stream);
+  JMG_CUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
+int jmg_op_smooth32_ws(JmgPlan* p, int level, int nsweeps, void* ws, size_t bytes, jmg_stream_t stream) {
+  int rc = check_ws(p, ws, bytes);
+  if (rc || (rc = level_check(p, level, false))) return rc;
+  if (!p->mixed) return set_err(JMG_ERR_VALUE, "jmg_op_smooth32_ws needs a plan with precision mixed");
+  Lvl<float> a = lvl32(p, ws, level);
+  for (int k = 0; k < nsweeps; ++k) launch_sweep<float>(p->dim, a, (cudaStream_t)stream);
   JMG_CUDA(cudaGetLastError());
   return JMG_OK;
 }

@@ -256,6 +256,86 @@ __global__ void __launch_bounds__(1024) k_coarse_cycle(const LvlTable<T>* tab, C
   blk_cycle<T, DIM>(tab, cp, lev, fcycle != 0, skip_pre != 0);
 }
 
+// FP32 2D coarse sub-cycle from shared memory. Every array of levels lev0 .. last (phi,
+// rhs, wx, wy, acc, invd; row pitch rp = nx rounded up to 4 floats) is staged in dynamic
+// shared memory with 16-byte loads, the recursion of blk_cycle then runs on shared-memory
+// views of the levels, and phi of lev0 is written back. Each pass of the cycle then costs
+// shared-memory latency instead of an L2 round trip, but the staging itself (~150 KB at
+// 2D 1024^2 per launch) costs more than that saves, so it is opt-in (JMG_COARSE32=smem).
+constexpr int kSmem32Max = 200 * 1024;
+
+__host__ __device__ inline int smem32_rp(int mx) { return (mx + 3 + 3) & ~3; }
+
+size_t coarse_smem32_bytes(const int* mx, const int* my, int lev0, int last) {
+  size_t n = 0;
+  for (int l = lev0; l <= last; ++l) n += (size_t)6 * smem32_rp(mx[l]) * (my[l] + 3);
+  return n * sizeof(float);
+}
+
+__global__ void __launch_bounds__(1024) k_coarse_smem32(const LvlTable<float>* tab, CycleParams cp, int lev0,
+                                                       int fcycle, int skip_pre) {
+  pdl_enter();
+  extern __shared__ __align__(16) float sm32[];
+  __shared__ LvlTable<float> st;
+  if (threadIdx.x == 0) {
+    size_t off = 0;
+    for (int l = lev0; l <= cp.last_level; ++l) {
+      Lvl<float> v = tab->l[l];
+      const int rp = smem32_rp(v.mx), ny = v.my + 3;
+      const size_t n = (size_t)rp * ny;
+      v.phi = sm32 + off;
+      v.rhs = v.phi + n;
+      v.wx = v.rhs + n;
+      v.wy = v.wx + n;
+      v.acc = v.wy + n;
+      v.invd = v.acc + n;
+      v.wz = nullptr;
+      v.xll = v.xrl = v.xlr = v.xrr = nullptr;
+      v.P = rp;
+      v.S = (long long)n;
+      st.l[l] = v;
+      off += 6 * n;
+    }
+  }
+  __syncthreads();
+  for (int l = lev0; l <= cp.last_level; ++l) {
+    const Lvl<float>& g = tab->l[l];
+    const Lvl<float>& v = st.l[l];
+    const int cpr = v.P / 4, ny = v.my + 3, n = cpr * ny;
+    const float* src[6] = {g.phi, g.rhs, g.wx, g.wy, g.acc, g.invd};
+    float* dst[6] = {v.phi, v.rhs, v.wx, v.wy, v.acc, v.invd};
+    for (int a = l == lev0 ? 0 : 2; a < 6; ++a)
+      for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int j = t / cpr, e = (t - j * cpr) * 4;
+        *reinterpret_cast<float4*>(dst[a] + j * v.P + e) =
+            __ldcg(reinterpret_cast<const float4*>(src[a] + (long long)j * g.P + e));
+      }
+  }
+  __syncthreads();
+  blk_cycle<float, 2>(&st, cp, lev0, fcycle != 0, skip_pre != 0);
+  {
+    const Lvl<float>& g = tab->l[lev0];
+    const Lvl<float>& v = st.l[lev0];
+    const int nx = v.mx + 3, n = nx * (v.my + 3);
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+      const int j = t / nx, i = t - j * nx;
+      g.phi[(long long)j * g.P + i] = v.phi[j * v.P + i];
+    }
+  }
+}
+
+int prepare_coarse_smem32(size_t bytes) {
+  return cudaFuncSetAttribute(k_coarse_smem32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) ==
+                 cudaSuccess
+             ? 0
+             : 1;
+}
+
+void launch_coarse_smem32(const LvlTable<float>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
+                          size_t smem, cudaStream_t s) {
+  launch_k(k_coarse_smem32, dim3(1), dim3(1024), smem, s, tab, cp, lev, fcycle, skip_pre);
+}
+
 template <typename T>
 __global__ void k_store_table(LvlTable<T> tab, LvlTable<T>* dst) {
   const int n = sizeof(LvlTable<T>) / sizeof(int);

@@ -80,6 +80,12 @@ template <typename T> int prepare_coarse_cluster(int dim, size_t smem_bytes, int
 template <typename T>
 void launch_coarse_cluster(int dim, const LvlTable<T>* tab, const ClusterLayout& lay, const CycleParams& cp,
                            int fcycle, int skip_pre, size_t smem_bytes, cudaStream_t s);
+// mg_kernels.cu: FP32 2D coarse sub-cycle with every array of the coarse levels staged in
+// shared memory (bytes from coarse_smem32_bytes; 0 from prepare_coarse_smem32 = usable)
+size_t coarse_smem32_bytes(const int* mx, const int* my, int lev0, int last);
+int prepare_coarse_smem32(size_t bytes);
+void launch_coarse_smem32(const LvlTable<float>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
+                          size_t smem, cudaStream_t s);
 // copies a level table into device memory (the coarse kernel reads it from there)
 template <typename T> void launch_store_table(const LvlTable<T>& tab, LvlTable<T>* dst, cudaStream_t s);
 
@@ -119,7 +125,8 @@ void launch_zero_f32(const Box& b, float* x, cudaStream_t s);
 void launch_convert_f32(const Box& b, const double* src, float* dst, cudaStream_t s);
 
 // mg_krylov.cu: FCG(1) around the cycle (outer = FCG)
-int fcg_num_parts();
+int fcg_num_parts();                                // partial-sum slots to reserve
+int fcg_parts_used(int dim, const Lvl<double>& a);  // partials a solve of this size writes
 // rho = rhs - L x (x = a.phi), d = q = 0, r32 = float(rho) (nullable); partials of rho^2
 void launch_fcg_init(int dim, const Lvl<double>& a, double* rho, double* d, double* q, float* r32, double* parts,
                      cudaStream_t s);

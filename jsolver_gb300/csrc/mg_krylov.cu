@@ -20,7 +20,12 @@ namespace jmg {
 
 namespace {
 
-constexpr int kBlocks = 304;  // fixed, so the reduction order is fixed
+// Block count of the FCG kernels: 304 (2 per SM) for up to 4096 interior rows, 1216 (8
+// per SM) above, where the vectors are large enough for the extra parallelism to pay for
+// the longer reductions. It depends on the problem size only, so for a given problem the
+// reduction order is fixed and solves are bitwise reproducible.
+constexpr int kBlocks = 1216;  // the most blocks (partials) any FCG kernel uses
+__host__ __device__ inline int fcg_blocks(int rows) { return rows > 4096 ? 1216 : 304; }
 constexpr int kThreads = 256;
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -52,7 +57,7 @@ __device__ __forceinline__ void totals2(const double* parts, double* t0, double*
   __shared__ double s[2];
   if (threadIdx.x < 32) {
     double a = 0.0, b = 0.0;
-    for (int t = threadIdx.x; t < kBlocks; t += 32) {
+    for (int t = threadIdx.x; t < (int)gridDim.x; t += 32) {
       a += parts[2 * t];
       b += parts[2 * t + 1];
     }
@@ -82,7 +87,7 @@ __device__ __forceinline__ long long row_base(const Lvl<double>& a, int r) {
   return DIM == 2 ? (long long)j * a.P : (long long)k * a.S + (long long)j * a.P;
 }
 #define JMG_FOR_POINTS(a, p)                                                          \
-  for (int r_ = blockIdx.x; r_ < nrows<DIM>(a); r_ += kBlocks)                        \
+  for (int r_ = blockIdx.x; r_ < nrows<DIM>(a); r_ += gridDim.x)                      \
     for (long long base_ = row_base<DIM>(a, r_), i_ = 2 + threadIdx.x; i_ <= (a).mx; \
          i_ += kThreads)                                                              \
       if (const long long p = base_ + i_; true)
@@ -298,49 +303,58 @@ __global__ void __launch_bounds__(kThreads) k_fcg32_x(Lvl<double> a, const float
 
 }  // namespace
 
+static int blocks_for(int dim, const Lvl<double>& a) {
+  return fcg_blocks((a.my - 1) * (dim == 3 ? a.mz - 1 : 1));
+}
+
 int fcg_num_parts() { return kBlocks; }
+int fcg_parts_used(int dim, const Lvl<double>& a) { return blocks_for(dim, a); }
 
 void launch_fcg32_init(int dim, const Lvl<double>& a, float* r32, float* d, float* q, double* parts,
                        cudaStream_t s) {
-  if (dim == 2) launch_k(k_fcg32_init<2>, dim3(kBlocks), dim3(kThreads), 0, s, a, r32, d, q, parts);
-  else launch_k(k_fcg32_init<3>, dim3(kBlocks), dim3(kThreads), 0, s, a, r32, d, q, parts);
+  const int nb = blocks_for(dim, a);
+  if (dim == 2) launch_k(k_fcg32_init<2>, dim3(nb), dim3(kThreads), 0, s, a, r32, d, q, parts);
+  else launch_k(k_fcg32_init<3>, dim3(nb), dim3(kThreads), 0, s, a, r32, d, q, parts);
 }
 
 // one step after the cycle produced z (FP32): dots, directions, x update, true residual
 void launch_fcg32_iter(int dim, const Lvl<double>& a, const Lvl<float>& a32, const float* z, float* d, float* q,
                        float* r32, double* parts_dots, double* parts_dir, double* parts_res, cudaStream_t s) {
+  const int nb = blocks_for(dim, a);
   if (dim == 2) {
-    launch_k(k_fcg32_dots<2>, dim3(kBlocks), dim3(kThreads), 0, s, a, z, d, q, parts_dots);
-    launch_k(k_fcg32_dir<2>, dim3(kBlocks), dim3(kThreads), 0, s, a, a32, z, d, q, r32, parts_dots, parts_dir);
-    launch_k(k_fcg32_x<2>, dim3(kBlocks), dim3(kThreads), 0, s, a, d, parts_dir);
-    launch_k(k_fcg32_init<2>, dim3(kBlocks), dim3(kThreads), 0, s, a, r32, (float*)nullptr, (float*)nullptr,
+    launch_k(k_fcg32_dots<2>, dim3(nb), dim3(kThreads), 0, s, a, z, d, q, parts_dots);
+    launch_k(k_fcg32_dir<2>, dim3(nb), dim3(kThreads), 0, s, a, a32, z, d, q, r32, parts_dots, parts_dir);
+    launch_k(k_fcg32_x<2>, dim3(nb), dim3(kThreads), 0, s, a, d, parts_dir);
+    launch_k(k_fcg32_init<2>, dim3(nb), dim3(kThreads), 0, s, a, r32, (float*)nullptr, (float*)nullptr,
              parts_res);
   } else {
-    launch_k(k_fcg32_dots<3>, dim3(kBlocks), dim3(kThreads), 0, s, a, z, d, q, parts_dots);
-    launch_k(k_fcg32_dir<3>, dim3(kBlocks), dim3(kThreads), 0, s, a, a32, z, d, q, r32, parts_dots, parts_dir);
-    launch_k(k_fcg32_x<3>, dim3(kBlocks), dim3(kThreads), 0, s, a, d, parts_dir);
-    launch_k(k_fcg32_init<3>, dim3(kBlocks), dim3(kThreads), 0, s, a, r32, (float*)nullptr, (float*)nullptr,
+    launch_k(k_fcg32_dots<3>, dim3(nb), dim3(kThreads), 0, s, a, z, d, q, parts_dots);
+    launch_k(k_fcg32_dir<3>, dim3(nb), dim3(kThreads), 0, s, a, a32, z, d, q, r32, parts_dots, parts_dir);
+    launch_k(k_fcg32_x<3>, dim3(nb), dim3(kThreads), 0, s, a, d, parts_dir);
+    launch_k(k_fcg32_init<3>, dim3(nb), dim3(kThreads), 0, s, a, r32, (float*)nullptr, (float*)nullptr,
              parts_res);
   }
 }
 
 void launch_fcg_init(int dim, const Lvl<double>& a, double* rho, double* d, double* q, float* r32, double* parts,
                      cudaStream_t s) {
-  if (dim == 2) launch_k(k_fcg_init<2>, dim3(kBlocks), dim3(kThreads), 0, s, a, rho, d, q, r32, parts);
-  else launch_k(k_fcg_init<3>, dim3(kBlocks), dim3(kThreads), 0, s, a, rho, d, q, r32, parts);
+  const int nb = blocks_for(dim, a);
+  if (dim == 2) launch_k(k_fcg_init<2>, dim3(nb), dim3(kThreads), 0, s, a, rho, d, q, r32, parts);
+  else launch_k(k_fcg_init<3>, dim3(nb), dim3(kThreads), 0, s, a, rho, d, q, r32, parts);
 }
 
 template <typename TZ>
 void launch_fcg_iter(int dim, const Lvl<double>& a, const TZ* z, double* d, double* q, double* rho, float* r32,
                      double* parts_dots, double* parts_dir, double* parts_res, cudaStream_t s) {
+  const int nb = blocks_for(dim, a);
   if (dim == 2) {
-    launch_k(k_fcg_dots<2, TZ>, dim3(kBlocks), dim3(kThreads), 0, s, a, z, d, q, parts_dots);
-    launch_k(k_fcg_dir<2, TZ>, dim3(kBlocks), dim3(kThreads), 0, s, a, z, d, q, rho, parts_dots, parts_dir);
-    launch_k(k_fcg_step<2>, dim3(kBlocks), dim3(kThreads), 0, s, a, d, q, rho, r32, parts_dir, parts_res);
+    launch_k(k_fcg_dots<2, TZ>, dim3(nb), dim3(kThreads), 0, s, a, z, d, q, parts_dots);
+    launch_k(k_fcg_dir<2, TZ>, dim3(nb), dim3(kThreads), 0, s, a, z, d, q, rho, parts_dots, parts_dir);
+    launch_k(k_fcg_step<2>, dim3(nb), dim3(kThreads), 0, s, a, d, q, rho, r32, parts_dir, parts_res);
   } else {
-    launch_k(k_fcg_dots<3, TZ>, dim3(kBlocks), dim3(kThreads), 0, s, a, z, d, q, parts_dots);
-    launch_k(k_fcg_dir<3, TZ>, dim3(kBlocks), dim3(kThreads), 0, s, a, z, d, q, rho, parts_dots, parts_dir);
-    launch_k(k_fcg_step<3>, dim3(kBlocks), dim3(kThreads), 0, s, a, d, q, rho, r32, parts_dir, parts_res);
+    launch_k(k_fcg_dots<3, TZ>, dim3(nb), dim3(kThreads), 0, s, a, z, d, q, parts_dots);
+    launch_k(k_fcg_dir<3, TZ>, dim3(nb), dim3(kThreads), 0, s, a, z, d, q, rho, parts_dots, parts_dir);
+    launch_k(k_fcg_step<3>, dim3(nb), dim3(kThreads), 0, s, a, d, q, rho, r32, parts_dir, parts_res);
   }
 }
 

@@ -58,6 +58,9 @@ struct JmgPlan {
   bool force_block = true;    // single-block coarse kernel (JMG_COARSE=cluster at plan creation: cluster)
   jmg::ClusterLayout cluster{};
   size_t cluster_smem64 = 0, cluster_smem32 = 0;
+  // FP32 2D coarse levels from shared memory (k_coarse_smem32, opt-in JMG_COARSE32=smem):
+  // its dynamic shared-memory bytes, 0 when not used
+  size_t coarse_smem32 = 0;
 };
 
 

@@ -499,3 +499,21 @@ def test_fcg_outer_fixed_count_and_errors():
     assert c == 7 and np.all(np.isfinite(phi))
     with pytest.raises(ValueError, match="fcg"):
         solve_2d(g, g, *args, outer="fcg")  # the distance stop measures a stationary iteration
+
+
+@pytest.mark.parametrize("m,form", [(1024, {}), (256, {"gamma": 2}), (128, {"fcycle": True}), (64, {"skip_pre": True}),
+                                    (512, {"outer": "fcg"})])
+def test_mixed_coarse_from_shared_memory_matches_global(m, form, monkeypatch):
+    """FP32 2D coarse levels staged in shared memory (opt-in, JMG_COARSE32=smem) against
+    the default recursion reading global memory: identical arithmetic, so the same cycle
+    count and phi to rounding."""
+    p = W.random_2d(m, seed=4)
+    g = grid_1D(m)
+    args = (p["phi0"], p["rhs"], p["lam"], p["D_xx"], p["D_yy"])
+    kw = dict(stop="residual", rtol=1e-10, precision="mixed", **form)
+    phi_g, c_g = solve_2d(g, g, *args, **kw)
+    monkeypatch.setenv("JMG_COARSE32", "smem")
+    monkeypatch.setattr(_engine, "CACHE", _engine._Cache())
+    phi_s, c_s = solve_2d(g, g, *args, **kw)
+    assert int(c_s) == int(c_g)
+    assert rel_l2(phi_s, phi_g) < 1e-13, rel_l2(phi_s, phi_g)
