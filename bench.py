@@ -56,7 +56,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="auto", choices=["auto", "fp64", "mixed", "learned", "learned-mixed"])
     ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 comparison solve")
-    ap.add_argument("--inner-cycles", type=int, default=1, help="FP32 cycles per refinement step (mixed forms)")
+    ap.add_argument("--inner-cycles", type=int, default=None,
+                    help="FP32 cycles per refinement / FCG step (mixed forms; default 2 with FCG, else 1)")
     ap.add_argument("--outer", default="auto", choices=["auto", "richardson", "fcg"],
                     help="iterate the cycle (reference) or use it as the preconditioner of flexible CG; "
                          "auto: fcg for the mixed and learned forms, richardson for fp64")
@@ -75,6 +76,10 @@ def parse():
         a.form = "mixed"
     if a.outer == "auto":
         a.outer = "richardson" if a.form == "fp64" else "fcg"
+    if a.inner_cycles is None:
+        # two V-cycles per FCG step amortise the step's FP64 vector work (2D 1024^2:
+        # 9.1 vs 9.4 ms; 3D 256^3 F-cycles: even)
+        a.inner_cycles = 2 if a.outer == "fcg" and a.form in ("mixed", "learned-mixed") else 1
     return a
 
 

@@ -168,6 +168,18 @@ int jmg_solve_fixed_vjp(JmgPlan* plan, const double* phi0, const double* rhs, co
                         double* Dxx_bar, double* Dyy_bar, void* workspace, size_t workspace_bytes,
                         void* adjoint_workspace, size_t adjoint_workspace_bytes, jmg_stream_t stream);
 
+/* Forward mode of the fixed-mode 2D solve (jax.jvp through solve_2d with fixed=True,
+ * solver_2d.py:461-463): phi and its tangent phi_dot for tangents phi0_dot, rhs_dot and
+ * the coefficient tangents coeffs_dot (lam, D_xx, D_yy; arrays where coeffs has arrays,
+ * scalars where it has scalars). FP64, 5-point stencil, the reference's iteration.
+ * tangent_workspace (jmg_tangent_workspace_bytes, the plan's workspace size) holds the
+ * tangent arrays in the plan's layout. */
+size_t jmg_tangent_workspace_bytes(const JmgPlan* plan);
+int jmg_solve_fixed_jvp(JmgPlan* plan, const double* phi0, const double* rhs, const JmgCoeffs* coeffs,
+                        const double* phi0_dot, const double* rhs_dot, const JmgCoeffs* coeffs_dot,
+                        double* phi_out, double* phi_dot_out, void* workspace, size_t workspace_bytes,
+                        void* tangent_workspace, size_t tangent_workspace_bytes, jmg_stream_t stream);
+
 /* Runs nsweeps red-black sweeps in place on the level arrays already in the workspace
  * (phi and rhs of that level as left by jmg_solve / jmg_op_*): the smoother of
  * red_black_gauss_seidel (solver_2d.py:670-692) without copies, for timing it alone. */

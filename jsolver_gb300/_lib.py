@@ -61,6 +61,9 @@ _SIGS = {
     "jmg_plan_launch_counts": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
     "jmg_rel_residual_noalloc": (ctypes.c_int, [ctypes.POINTER(JmgGrid), _P, _P, ctypes.POINTER(JmgCoeffs), _P, _P]),
     "jmg_adjoint_workspace_bytes": (ctypes.c_size_t, [_P]),
+    "jmg_tangent_workspace_bytes": (ctypes.c_size_t, [_P]),
+    "jmg_solve_fixed_jvp": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(JmgCoeffs), _P, _P, ctypes.POINTER(JmgCoeffs), _P,
+                                           _P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, _P]),
     "jmg_solve_fixed_vjp": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(JmgCoeffs), _P, _P, _P, _P, _P, _P, _P,
                                            ctypes.c_size_t, _P, ctypes.c_size_t, _P]),
     "jmg_net_num_params": (ctypes.c_int64, []),
