@@ -41,6 +41,7 @@ RTOL = 1e-10
 WORKLOADS = {  # name -> (dimension, default resolution, default cycle)
     "2d": (2, 1024, "V"),  # 2D 1024^2 random-coefficient problem (arrays 1027^2 float64)
     "3d": (3, 256, "F"),   # 3D 256^3 random-coefficient problem (arrays 259^3 float64)
+    "adjoint": (2, 512, "V"),  # reverse mode: 2D 512^2, fixed 12 V-cycles, loss sum(w phi)
 }
 
 
@@ -239,8 +240,69 @@ def cpu_baseline(p, dim, m, cycles_needed, kw, budget_s=20.0):
                       f"{cycles_needed} cycles a solve to 1e-10 takes"}
 
 
+def adjoint_bench(args):
+    """Reverse mode of the fixed-mode 2D solve: forward (12 V-cycles) and backward (the
+    hand-written adjoint) device times, their ratio and the peak device memory of one
+    forward + backward, on the 2D random-coefficient problem at 512^2, loss = sum(w phi)
+    with seeded Gaussian weights w."""
+    import torch
+    from jsolver_gb300 import workloads
+    from jsolver_gb300.grid_1d import grid_1D
+    from jsolver_gb300.solver_2d import solve_2d
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    m, iters = args.m, 12
+    p = workloads.random_2d(m, seed=args.seed)
+    g = grid_1D(m)
+    w = torch.from_numpy(np.random.default_rng(args.seed + 1).standard_normal(p["rhs"].shape)).to(dev)
+    names = ("phi0", "rhs", "lam", "D_xx", "D_yy")
+
+    def inputs(grad):
+        return [torch.from_numpy(p[k]).to(dev).requires_grad_(grad and k != "phi0") for k in names]
+
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    fwd, bwd = [], []
+    for it in range(args.warmup + args.steps):
+        x = inputs(False)
+        e0, e1 = ev(), ev()
+        e0.record()
+        with torch.no_grad():
+            solve_2d(g, g, *x, fixed=True, max_iters_outer=iters)
+        e1.record()
+        x = inputs(True)
+        phi, _ = solve_2d(g, g, *x, fixed=True, max_iters_outer=iters)
+        loss = (phi * w).sum()
+        e2, e3 = ev(), ev()
+        e2.record()
+        loss.backward()
+        e3.record()
+        torch.cuda.synchronize()
+        if it >= args.warmup:
+            fwd.append(e0.elapsed_time(e1))
+            bwd.append(e2.elapsed_time(e3))
+    torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats(dev)
+    base = torch.cuda.memory_allocated(dev)
+    x = inputs(True)
+    phi, _ = solve_2d(g, g, *x, fixed=True, max_iters_outer=iters)
+    (phi * w).sum().backward()
+    torch.cuda.synchronize()
+    peak = torch.cuda.max_memory_allocated(dev) - base
+    f, b = float(np.median(fwd)), float(np.median(bwd))
+    line = {"metric": f"backward/forward time ratio, reverse mode of the fixed-mode 2D solve ({m}^2, {iters} V-cycles)",
+            "value": b / f, "unit": "ratio", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": False, "dtype": "f64", "data": "synthetic (seeded GRF coefficients, manufactured rhs)",
+            "config": {"workload": f"2d-{m}^2-random-coeff fixed {iters} V-cycles, loss = sum(w phi)",
+                       "gradients": "rhs, lam, D_xx, D_yy (and phi0)"},
+            "forward_ms": f, "backward_ms": b, "peak_device_memory_mb": peak / 2 ** 20,
+            "array_mb": p["rhs"].nbytes / 2 ** 20}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "adjoint":
+        return adjoint_bench(args)
     if args.impl == "reference":
         return reference_arm(args)
     import torch
