@@ -51,9 +51,14 @@ int set_err(int code, const char* fmt, ...) {
 // First level run by the single-block global-memory coarse kernel: at most 8192 padded
 // points, and never below the last visited level.
 int block_coarse_start(const JmgPlan* p) {
+  static const long long limit = [] {
+    const char* e = getenv("JMG_COARSE_POINTS");  // tuning knob; 8192 by default
+    const long long v = e ? atoll(e) : 0;
+    return v > 0 ? v : 8192LL;
+  }();
   for (int l = 0; l < p->used; ++l) {
     const long long pts = (long long)p->lv[l].box.nx * p->lv[l].box.ny * p->lv[l].box.nz;
-    if (pts <= 8192) return l;
+    if (pts <= limit) return l;
   }
   return p->used - 1;
 }

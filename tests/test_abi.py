@@ -49,3 +49,38 @@ def test_too_small_grid_is_a_value_error():
     import pytest
     with pytest.raises(ValueError, match="too small"):
         _lib.Plan(_engine.make_grid((grid_1D(1), grid_1D(1))), _engine.make_config())
+
+
+def test_config_extensions_are_validated_without_gpu():
+    """outer='fcg' needs the residual stop or a fixed count; off_diag is 2D only; the
+    workspace grows by the FCG vectors and the D_xy diagonals (plan layout is host-only)."""
+    import pytest
+    g2 = _engine.make_grid((grid_1D(64), grid_1D(64)))
+    g3 = _engine.make_grid((grid_1D(16),) * 3)
+    with pytest.raises(ValueError, match="fcg"):
+        _lib.Plan(g2, _engine.make_config(outer="fcg"))
+    with pytest.raises(ValueError, match="outer"):
+        _engine.make_config(outer="gmres")
+    with pytest.raises(ValueError, match="2D"):
+        _lib.Plan(g3, _engine.make_config(off_diag=True))
+    base = _lib.Plan(g2, _engine.make_config(stop="residual")).workspace_bytes
+    fcg = _lib.Plan(g2, _engine.make_config(stop="residual", outer="fcg")).workspace_bytes
+    fixed_fcg = _lib.Plan(g2, _engine.make_config(fixed=True, outer="fcg")).workspace_bytes
+    dxy = _lib.Plan(g2, _engine.make_config(off_diag=True)).workspace_bytes
+    n0 = 67 * 80 * 8  # level-0 FP64 array (pitch 80)
+    assert fcg >= base + 4 * n0 and fixed_fcg == fcg
+    assert dxy >= base + 4 * n0  # four diagonal couplings per level
+
+
+def test_launch_counts_follow_the_form():
+    lib = _lib.load()
+    g = _engine.make_grid((grid_1D(1024), grid_1D(1024)))
+    counts = {}
+    for name, cfg in (("plain", _engine.make_config(stop="residual")),
+                      ("fcg", _engine.make_config(stop="residual", precision="mixed", outer="fcg"))):
+        p = _lib.Plan(g, cfg)
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        assert lib.jmg_plan_launch_counts(p.handle, ctypes.byref(a), ctypes.byref(b)) == 0
+        counts[name] = b.value
+    # an FCG step adds its four vector kernels to the cycle and the stopping test
+    assert counts["fcg"] >= counts["plain"] + 3
