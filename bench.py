@@ -42,6 +42,7 @@ WORKLOADS = {  # name -> (dimension, default resolution, default cycle)
     "2d": (2, 1024, "V"),  # 2D 1024^2 random-coefficient problem (arrays 1027^2 float64)
     "3d": (3, 256, "F"),   # 3D 256^3 random-coefficient problem (arrays 259^3 float64)
     "adjoint": (2, 512, "V"),  # reverse mode: 2D 512^2, fixed 12 V-cycles, loss sum(w phi)
+    "batch": (2, 256, "V"),  # many independent 2D 256^2 problems in one batched call
 }
 
 
@@ -68,6 +69,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--batch", type=int, default=64, help="problems per step of the batch workload")
+    ap.add_argument("--iters", type=int, default=12, help="fixed cycles of the adjoint workload")
+    ap.add_argument("--lanes", type=int, default=8, help="concurrent lanes of the batch workload")
     a = ap.parse_args()
     dim, m, cyc = WORKLOADS[a.workload]
     a.dim = dim
@@ -241,7 +245,7 @@ def cpu_baseline(p, dim, m, cycles_needed, kw, budget_s=20.0):
 
 
 def adjoint_bench(args):
-    """Reverse mode of the fixed-mode 2D solve: forward (12 V-cycles) and backward (the
+    """Reverse mode of the fixed-mode 2D solve: forward (--iters V-cycles, 12 by default) and backward (the
     hand-written adjoint) device times, their ratio and the peak device memory of one
     forward + backward, on the 2D random-coefficient problem at 512^2, loss = sum(w phi)
     with seeded Gaussian weights w."""
@@ -251,7 +255,7 @@ def adjoint_bench(args):
     from jsolver_gb300.solver_2d import solve_2d
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    m, iters = args.m, 12
+    m, iters = args.m, args.iters
     p = workloads.random_2d(m, seed=args.seed)
     g = grid_1D(m)
     w = torch.from_numpy(np.random.default_rng(args.seed + 1).standard_normal(p["rhs"].shape)).to(dev)
@@ -280,7 +284,12 @@ def adjoint_bench(args):
         if it >= args.warmup:
             fwd.append(e0.elapsed_time(e1))
             bwd.append(e2.elapsed_time(e3))
+    # the library keeps the solve's and the adjoint's workspaces across calls: release
+    # them so that the measured peak includes both
+    from jsolver_gb300 import _engine
     torch.cuda.synchronize()
+    _engine.CACHE.ws.clear()
+    torch.cuda.empty_cache()
     torch.cuda.reset_peak_memory_stats(dev)
     base = torch.cuda.memory_allocated(dev)
     x = inputs(True)
@@ -299,10 +308,70 @@ def adjoint_bench(args):
     print(json.dumps(line), flush=True)
 
 
+def batch_bench(args):
+    """Many independent solves: ``--batch`` 2D random-coefficient problems at ``--m``
+    (256 by default; seeds seed..seed+B-1), each to rel. residual 1e-10, in one
+    solve_2d_batched call with ``--lanes`` concurrent lanes, against the same problems
+    solved one after another with solve_2d. Inputs resident on the device, L2 flushed
+    before every timed step, CUDA events on the calling stream."""
+    import torch
+    from jsolver_gb300 import workloads
+    from jsolver_gb300.grid_1d import grid_1D
+    from jsolver_gb300.solver_2d import solve_2d, solve_2d_batched
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    m, nb = args.m, args.batch
+    g = grid_1D(m)
+    probs = [workloads.random_2d(m, seed=args.seed + b) for b in range(nb)]
+    keys = ("phi0", "rhs", "lam", "D_xx", "D_yy")
+    X = [torch.from_numpy(np.stack([p[k] for p in probs])).to(dev) for k in keys]
+    precision = "mixed" if args.form in ("mixed", "learned-mixed") else "fp64"
+    opts = dict(stop="residual", rtol=RTOL, precision=precision, max_iters_outer=20000, outer=args.outer,
+                **cycle_kw(args.cycle))
+    if precision == "mixed":
+        opts["inner_cycles"] = args.inner_cycles
+    flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device=dev)
+
+    def timed(fn):
+        out = []
+        for it in range(args.warmup + args.steps):
+            flush.fill_(it & 0xFF)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            if it >= args.warmup:
+                out.append(e0.elapsed_time(e1))
+        return float(np.median(out)), r
+
+    t_b, (phi_b, cnt_b) = timed(lambda: solve_2d_batched(g, g, *X, lanes=args.lanes, **opts))
+
+    def sequential():
+        res = [solve_2d(g, g, *[x[b] for x in X], **opts) for b in range(nb)]
+        return res
+
+    t_s, res_s = timed(sequential)
+    same = all(torch.equal(phi_b[b], res_s[b][0]) and int(cnt_b[b]) == int(res_s[b][1]) for b in range(nb))
+    line = {"metric": f"solves/s, {nb} independent 2D {m}^2 random-coefficient problems to rel. residual 1e-10",
+            "value": nb / (t_b / 1e3), "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "dtype": "f32+f64" if precision == "mixed" else "f64",
+            "data": "synthetic (seeded GRF coefficients, manufactured rhs)",
+            "config": {"workload": f"batch of {nb} 2d-{m}^2-random-coeff, {args.cycle}-cycles, "
+                                   f"{precision}, outer {args.outer}", "lanes": args.lanes,
+                       "l2": "flushed (256 MB write) before every step"},
+            "ms_per_batch": t_b, "sequential_ms": t_s, "sequential_solves_per_s": nb / (t_s / 1e3),
+            "speedup_vs_sequential": t_s / t_b, "cycles_mean": float(cnt_b.double().mean()),
+            "identical_to_single_solves": bool(same)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "adjoint":
         return adjoint_bench(args)
+    if args.workload == "batch":
+        return batch_bench(args)
     if args.impl == "reference":
         return reference_arm(args)
     import torch

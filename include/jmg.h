@@ -108,6 +108,31 @@ int jmg_solve(JmgPlan* plan, const double* phi0, const double* rhs, const JmgCoe
               double* phi_out, int64_t* count_out, void* workspace, size_t workspace_bytes,
               jmg_stream_t stream);
 
+/* Element strides between consecutive problems of a batch, per coefficient array; 0 means
+ * the array is shared by every problem. Scalars (NULL arrays) ignore their stride. */
+typedef struct JmgBatchStrides {
+  int64_t lam;
+  int64_t D[3];
+  int64_t D_xy;
+} JmgBatchStrides;
+
+/* Workspace of a batched solve that runs `lanes` problems side by side (at most 32):
+ * lanes x the plan's workspace, each slice aligned. */
+size_t jmg_batched_workspace_bytes(const JmgPlan* plan, int32_t lanes);
+
+/* batch independent solves of one plan (jax.vmap of solve_2d / solve_3d in the
+ * reference's variational-inference use, README.md:107, examples/benchmark.py:1109-1230).
+ * phi0, rhs and phi_out hold batch dense padded arrays back to back; coefficient
+ * pointers address problem 0 and advance by strides per problem. counts_out: device
+ * int64[batch] (or NULL). The workspace's size sets the number of lanes
+ * (workspace_bytes / jmg_batched_workspace_bytes(plan, 1), at most 32 and at most batch);
+ * the lanes run on the plan's own streams, forked from and joined back to `stream`.
+ * Each problem's phi and count equal those of jmg_solve on it alone. */
+int jmg_solve_batched(JmgPlan* plan, int32_t batch, const double* phi0, const double* rhs,
+                      const JmgCoeffs* coeffs, const JmgBatchStrides* strides, double* phi_out,
+                      int64_t* counts_out, void* workspace, size_t workspace_bytes,
+                      jmg_stream_t stream);
+
 /* One-shot form of jmg_solve for 2D / 3D (creates and destroys a plan). */
 int jmg_solve2d_f64(const JmgGrid* grid, const JmgConfig* cfg, const double* phi0,
                     const double* rhs, const JmgCoeffs* coeffs, double* phi_out,

@@ -90,12 +90,15 @@ class _Cache:
                 self.plans[key] = p
             return p
 
-    def workspace(self, plan, device):
-        key = (id(plan), str(device))
+    def workspace(self, plan, device, kind="solve", nbytes=None):
+        """Device workspace of a plan, kept across calls (a stable address lets the
+        library reuse the graphs it captured for that address)."""
+        nbytes = plan.workspace_bytes if nbytes is None else nbytes
+        key = (id(plan), str(device), kind)
         with self.lock:
             w = self.ws.get(key)
-            if w is None or w.numel() < plan.workspace_bytes:
-                w = torch.empty(max(plan.workspace_bytes, 1), dtype=torch.uint8, device=device)
+            if w is None or w.numel() < nbytes:
+                w = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=device)
                 self.ws[key] = w
             return w
 
@@ -208,6 +211,65 @@ def solve(grids, phi, rhs, lam, D, D_xy=None, guess=None, **opts):
         if torch_in:
             return out, (int(cfg.max_iters_outer) if cfg.fixed else count)
         return out.cpu().numpy(), (int(cfg.max_iters_outer) if cfg.fixed else int(count.item()))
+
+
+def solve_batched(grids, phi, rhs, lam, D, D_xy=None, lanes=8, **opts):
+    """B independent solves of one grid through ``jmg_solve_batched``.
+
+    ``phi`` and ``rhs`` have shape (B, *spatial); ``lam`` and every D component are a
+    scalar, one array of the spatial shape shared by all problems, or a (B, *spatial)
+    array (the reference's jax.vmap over solve_2d / solve_3d with those in_axes). ``lanes``
+    problems run side by side, each on its own workspace and stream. Returns ``(phi,
+    counts)`` with counts an int64 array of length B; problem b's results are those of
+    ``solve`` on problem b alone."""
+    ndim = len(grids)
+    grid = make_grid(grids)
+    CACHE.plan(grid, make_config(**opts))  # grid checks first
+    spatial_shape = expected_shape(grids)
+    ps, rs = shape_of(phi), shape_of(rhs)
+    if len(ps) != ndim + 1 or ps != rs or ps[0] < 1:
+        raise ValueError(f"Shape mismatch: batched phi and rhs must both have shape (B, "
+                         f"{', '.join(map(str, spatial_shape))}) with B >= 1, got phi={ps}, rhs={rs}.")
+    nb = ps[0]
+    coeffs = [lam] + list(D) + ([] if D_xy is None else [D_xy])
+
+    def batched(x):
+        return not is_scalar(x) and len(shape_of(x)) == ndim + 1
+
+    for x in coeffs:
+        if batched(x) and shape_of(x)[0] != nb:
+            raise ValueError(f"Shape mismatch: batched coefficient of shape {shape_of(x)} for a batch of {nb}.")
+
+    def first(x):  # problem 0's view
+        return x[0] if batched(x) else x
+
+    sl, spatial, off = validate(ndim, phi[0], rhs[0], first(lam), [first(d) for d in D],
+                                None if D_xy is None else first(D_xy), spatial_shape)
+    cfg = make_config(off_diag=off, **opts)
+    plan = CACHE.plan(grid, cfg)
+    torch_in = any(is_cuda_tensor(a) for a in [phi, rhs] + coeffs)
+    device = pick_device(phi, rhs, *coeffs)
+    lib = _lib.load()
+    npts = int(np.prod(spatial_shape))
+    with torch.cuda.device(device):
+        phi_d = to_device(phi, device)
+        rhs_d = to_device(rhs, device)
+        prep = Prepared(ndim, device, lam, D, D_xy, sl, spatial)
+        st = _lib.JmgBatchStrides()
+        st.lam = npts if (not sl and batched(lam)) else 0
+        for a in range(ndim):
+            st.D[a] = npts if (spatial and batched(D[a])) else 0
+        st.D_xy = npts if (off and batched(D_xy)) else 0
+        out = torch.empty_like(phi_d)
+        counts = torch.empty(nb, dtype=torch.int64, device=device)
+        lanes = max(1, min(int(lanes), nb, 32))
+        ws = CACHE.workspace(plan, device, "batch", lib.jmg_batched_workspace_bytes(plan.handle, lanes))
+        _lib.check(lib.jmg_solve_batched(plan.handle, nb, _ptr(phi_d), _ptr(rhs_d), ctypes.byref(prep.coeffs),
+                                         ctypes.byref(st), _ptr(out), _ptr(counts), _ptr(ws),
+                                         ctypes.c_size_t(ws.numel()), _stream_ptr(device)))
+        if torch_in:
+            return out, counts
+        return out.cpu().numpy(), counts.cpu().numpy()
 
 
 class OperatorSet:

@@ -35,6 +35,10 @@ class JmgCoeffs(ctypes.Structure):
                 ("D", ctypes.c_void_p * 3), ("D_scalar", ctypes.c_double * 3), ("D_xy", ctypes.c_void_p)]
 
 
+class JmgBatchStrides(ctypes.Structure):
+    _fields_ = [("lam", ctypes.c_int64), ("D", ctypes.c_int64 * 3), ("D_xy", ctypes.c_int64)]
+
+
 # every symbol of include/jmg.h with its ctypes signature
 _P = ctypes.c_void_p
 _SIGS = {
@@ -44,6 +48,9 @@ _SIGS = {
     "jmg_plan_workspace_bytes": (ctypes.c_size_t, [_P]),
     "jmg_plan_levels": (ctypes.c_int, [_P]),
     "jmg_solve": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(JmgCoeffs), _P, _P, _P, ctypes.c_size_t, _P]),
+    "jmg_batched_workspace_bytes": (ctypes.c_size_t, [_P, ctypes.c_int32]),
+    "jmg_solve_batched": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P, ctypes.POINTER(JmgCoeffs),
+                                         ctypes.POINTER(JmgBatchStrides), _P, _P, _P, ctypes.c_size_t, _P]),
     "jmg_solve2d_f64": (ctypes.c_int, [ctypes.POINTER(JmgGrid), ctypes.POINTER(JmgConfig), _P, _P,
                                        ctypes.POINTER(JmgCoeffs), _P, _P, _P, ctypes.c_size_t, _P]),
     "jmg_solve3d_f64": (ctypes.c_int, [ctypes.POINTER(JmgGrid), ctypes.POINTER(JmgConfig), _P, _P,

@@ -44,7 +44,7 @@ class FixedSolve2D(torch.autograd.Function):
         dev = phi0.device
         ws = _engine.CACHE.workspace(plan, dev)
         abytes = lib.jmg_adjoint_workspace_bytes(plan.handle)
-        aws = torch.empty(max(abytes, 1), dtype=torch.uint8, device=dev)
+        aws = _engine.CACHE.workspace(plan, dev, "adjoint", abytes)
         co = _lib.JmgCoeffs()
         co.lam = lam.data_ptr()
         co.D[0], co.D[1] = Dx.data_ptr(), Dy.data_ptr()

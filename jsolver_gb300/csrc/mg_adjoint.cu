@@ -148,6 +148,59 @@ void run_tape_forward(const JmgPlan* p, void* ws, void* aws, const AdjLayout& L,
     cudaMemcpyAsync(first.phi, cur[0].phi, p->lv[0].elems * 8, cudaMemcpyDeviceToDevice, s);
 }
 
+// the checkpointed forward (the one-off pre-smoothing, then n cycles keeping phi at the
+// start of each) and the reverse sweep over the cycles, newest first. Reads and writes only
+// the plan workspace ws and the adjoint workspace aws, so one capture serves every call
+// with the same two addresses. phi_0, rhs and the hierarchy are in ws, the input adjoint in
+// level 0's pb and every other adjoint array is zero when it starts.
+void adj_core(const JmgPlan* p, void* ws, void* aws, const AdjLayout& L, const Tape& tape, cudaStream_t s) {
+  const size_t e0 = p->lv[0].elems;
+  Lvl<double> l0 = lvl64(p, ws, 0);
+  const CycleParams cp = cycle_params(p, false);
+  const int nu1 = p->cfg.nu1 > 0 ? p->cfg.nu1 : 0;
+  double* pre = ptr<double>(aws, L.pre);
+  if (p->cfg.skip_pre) {  // the one-off pre-smoothing (solver_2d.py:457-459)
+    cudaMemcpyAsync(pre, l0.phi, e0 * 8, cudaMemcpyDeviceToDevice, s);
+    Lvl<double> cur = l0;
+    for (int k = 0; k < nu1; ++k) {
+      launch_sweep<double>(2, cur, s);
+      cudaMemcpyAsync(pre + (size_t)(k + 1) * e0, cur.phi, e0 * 8, cudaMemcpyDeviceToDevice, s);
+    }
+    if (cur.phi != l0.phi) cudaMemcpyAsync(l0.phi, cur.phi, e0 * 8, cudaMemcpyDeviceToDevice, s);
+  }
+  double* ck = ptr<double>(aws, L.ckpt);
+  for (int k = 0; k < L.ncyc; ++k) {
+    // the loop body starts with do_BCs (solver_2d.py:462); the level-0 frame is already zero
+    cudaMemcpyAsync(ck + (size_t)k * e0, l0.phi, e0 * 8, cudaMemcpyDeviceToDevice, s);
+    run_tape_forward(p, ws, aws, L, tape, false, s);
+  }
+  std::vector<AdjLvl> g(p->used);
+  for (int l = 0; l < p->used; ++l) g[l] = adj_lvl(p, aws, L, l);
+  const double* zeros = ptr<double>(aws, L.zeros);
+  for (int k = L.ncyc - 1; k >= 0; --k) {
+    cudaMemcpyAsync(l0.phi, ck + (size_t)k * e0, e0 * 8, cudaMemcpyDeviceToDevice, s);
+    run_tape_forward(p, ws, aws, L, tape, true, s);
+    auto state = [&](int idx) -> const double* {
+      if (idx == kZeros) return zeros;
+      if (idx == kInput) return ck + (size_t)k * e0;
+      return ptr<double>(aws, L.snap[idx]);
+    };
+    for (int t = (int)tape.ops.size() - 1; t >= 0; --t) {
+      const TapeOp& op = tape.ops[t];
+      Lvl<double> a = lvl64(p, ws, op.lev);
+      if (op.kind == OP_SWEEP) {
+        adj_sweep(a, g[op.lev], state(op.before), state(op.after), s);
+      } else if (op.kind == OP_PROLONG) {
+        adj_prolong(a, g[op.lev], lvl64(p, ws, op.lev + 1), g[op.lev + 1], cp.diag, s);
+      } else {
+        adj_restrict(a, g[op.lev], state(op.before), lvl64(p, ws, op.lev + 1), g[op.lev + 1], s);
+      }
+    }
+  }
+  if (p->cfg.skip_pre)
+    for (int k = nu1 - 1; k >= 0; --k) adj_sweep(l0, g[0], pre + (size_t)k * e0, pre + (size_t)(k + 1) * e0, s);
+}
+
 }  // namespace
 }  // namespace jmg
 
@@ -181,72 +234,51 @@ int jmg_solve_fixed_vjp(JmgPlan* p, const double* phi0, const double* rhs, const
     return fail(JMG_ERR_WORKSPACE, "adjoint workspace missing, too small or misaligned");
   cudaStream_t s = (cudaStream_t)stream;
   const Box b0 = p->lv[0].box;
-  const size_t e0 = p->lv[0].elems;
   const size_t dense = (size_t)b0.nx * b0.ny * b0.nz;
   Lvl<double> l0 = lvl64(p, ws, 0);
-  const CycleParams cp = cycle_params(p, false);
-  const int nu1 = p->cfg.nu1 > 0 ? p->cfg.nu1 : 0;
 
-  // forward with checkpoints
+  // the input adjoint and the zeroed adjoint state, then the checkpointed forward and the
+  // reverse sweep (one graph launch, or the same operations from the host)
   launch_copy_in(b0, phi0, l0.phi, 1, s);
   launch_copy_in(b0, rhs, l0.rhs, 1, s);
   if ((rc = build_hierarchy(p, c, ws, s))) return rc;
   JMG_ACUDA(cudaMemsetAsync(aws, 0, L.total, s));
-  double* pre = ptr<double>(aws, L.pre);
-  if (p->cfg.skip_pre) {  // the one-off pre-smoothing (solver_2d.py:457-459)
-    JMG_ACUDA(cudaMemcpyAsync(pre, l0.phi, e0 * 8, cudaMemcpyDeviceToDevice, s));
-    Lvl<double> cur = l0;
-    for (int k = 0; k < nu1; ++k) {
-      launch_sweep<double>(2, cur, s);
-      JMG_ACUDA(cudaMemcpyAsync(pre + (size_t)(k + 1) * e0, cur.phi, e0 * 8, cudaMemcpyDeviceToDevice, s));
-    }
-    if (cur.phi != l0.phi) JMG_ACUDA(cudaMemcpyAsync(l0.phi, cur.phi, e0 * 8, cudaMemcpyDeviceToDevice, s));
-  }
-  double* ck = ptr<double>(aws, L.ckpt);
-  for (int k = 0; k < L.ncyc; ++k) {
-    // the loop body starts with do_BCs (solver_2d.py:462); the level-0 frame is already zero
-    JMG_ACUDA(cudaMemcpyAsync(ck + (size_t)k * e0, l0.phi, e0 * 8, cudaMemcpyDeviceToDevice, s));
-    run_tape_forward(p, ws, aws, L, tape, false, s);
-  }
-
-  // backward
-  std::vector<AdjLvl> g(p->used);
-  for (int l = 0; l < p->used; ++l) g[l] = adj_lvl(p, aws, L, l);
-  launch_copy_in(b0, phi_bar, g[0].pb, 1, s);  // the output's frame is a constant (do_BCs)
-  const double* zeros = ptr<double>(aws, L.zeros);
-  for (int k = L.ncyc - 1; k >= 0; --k) {
-    JMG_ACUDA(cudaMemcpyAsync(l0.phi, ck + (size_t)k * e0, e0 * 8, cudaMemcpyDeviceToDevice, s));
-    run_tape_forward(p, ws, aws, L, tape, true, s);
-    auto state = [&](int idx, int lev) -> const double* {
-      if (idx == kZeros) return zeros;
-      if (idx == kInput) return ck + (size_t)k * e0;
-      (void)lev;
-      return ptr<double>(aws, L.snap[idx]);
-    };
-    for (int t = (int)tape.ops.size() - 1; t >= 0; --t) {
-      const TapeOp& op = tape.ops[t];
-      Lvl<double> a = lvl64(p, ws, op.lev);
-      if (op.kind == OP_SWEEP) {
-        adj_sweep(a, g[op.lev], state(op.before, op.lev), state(op.after, op.lev), s);
-      } else if (op.kind == OP_PROLONG) {
-        adj_prolong(a, g[op.lev], lvl64(p, ws, op.lev + 1), g[op.lev + 1], cp.diag, s);
-      } else {
-        adj_restrict(a, g[op.lev], state(op.before, op.lev), lvl64(p, ws, op.lev + 1), g[op.lev + 1], s);
+  launch_copy_in(b0, phi_bar, adj_lvl(p, aws, L, 0).pb, 1, s);  // the output's frame is a constant (do_BCs)
+  if (p->host_loop) {
+    adj_core(p, ws, aws, L, tape, s);
+  } else {
+    if (!p->vjp_exec || p->vjp_ws != ws || p->vjp_aws != aws) {
+      if (p->vjp_exec) {
+        cudaGraphExecDestroy(p->vjp_exec);
+        p->vjp_exec = nullptr;
       }
+      if (!p->cap) JMG_ACUDA(cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking));
+      JMG_ACUDA(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
+      adj_core(p, ws, aws, L, tape, p->cap);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ec = cudaStreamEndCapture(p->cap, &graph);
+      JMG_ACUDA(ec);
+      cudaGraphExec_t exec = nullptr;
+      const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      JMG_ACUDA(ei);
+      p->vjp_exec = exec;
+      p->vjp_ws = ws;
+      p->vjp_aws = aws;
     }
+    JMG_ACUDA(cudaGraphLaunch(p->vjp_exec, s));
   }
-  if (p->cfg.skip_pre)
-    for (int k = nu1 - 1; k >= 0; --k) adj_sweep(l0, g[0], pre + (size_t)k * e0, pre + (size_t)(k + 1) * e0, s);
+  const AdjLvl g0 = adj_lvl(p, aws, L, 0);
 
   // adjoints of the inputs: phi0, rhs (level 0), then the coefficient hierarchy
-  launch_copy_out(b0, g[0].pb, phi0_bar, s);
-  launch_copy_out(b0, g[0].rb, rhs_bar, s);
+  launch_copy_out(b0, g0.pb, phi0_bar, s);
+  launch_copy_out(b0, g0.rb, rhs_bar, s);
   JMG_ACUDA(cudaMemsetAsync(lam_bar, 0, dense * 8, s));
   JMG_ACUDA(cudaMemsetAsync(Dxx_bar, 0, dense * 8, s));
   JMG_ACUDA(cudaMemsetAsync(Dyy_bar, 0, dense * 8, s));
   for (int l = 0; l < p->used; ++l) {
     const double ix = p->grid.idel[0] * std::pow(0.5, l), iy = p->grid.idel[1] * std::pow(0.5, l);
-    adj_hierarchy2d(lvl64(p, ws, l), g[l], l, ix * ix, iy * iy, b0.nx, Dxx_bar, Dyy_bar, lam_bar, s);
+    adj_hierarchy2d(lvl64(p, ws, l), adj_lvl(p, aws, L, l), l, ix * ix, iy * iy, b0.nx, Dxx_bar, Dyy_bar, lam_bar, s);
   }
   JMG_ACUDA(cudaGetLastError());
   return JMG_OK;

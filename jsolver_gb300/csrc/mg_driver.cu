@@ -48,13 +48,16 @@ int set_err(int code, const char* fmt, ...) {
     if (e_ != cudaSuccess) return set_err(JMG_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
   } while (0)
 
-// First level run by the single-block global-memory coarse kernel: at most 8192 padded
-// points, and never below the last visited level.
+// First level run by the single-block global-memory coarse kernel: at most 2048 padded
+// points (2D 32^2, 3D 8^3 interiors), and never below the last visited level. Thresholds
+// of 256 to 8192 points measured on GB300: 2048 is fastest for the 2D and 3D solves in
+// FP64 and in mixed precision; at 8192 the block spends longer on the 64^2 / 16^3 level
+// than one grid-wide launch per operator takes.
 int block_coarse_start(const JmgPlan* p) {
   static const long long limit = [] {
-    const char* e = getenv("JMG_COARSE_POINTS");  // tuning knob; 8192 by default
+    const char* e = getenv("JMG_COARSE_POINTS");  // tuning knob; 2048 by default
     const long long v = e ? atoll(e) : 0;
-    return v > 0 ? v : 8192LL;
+    return v > 0 ? v : 2048LL;
   }();
   for (int l = 0; l < p->used; ++l) {
     const long long pts = (long long)p->lv[l].box.nx * p->lv[l].box.ny * p->lv[l].box.nz;
@@ -185,7 +188,7 @@ int validate_and_layout(JmgPlan* p) {
 
 }  // namespace
 // How the coarse levels of a cycle run. By default one block runs the levels of at most
-// 8192 points from global memory. With JMG_COARSE=cluster (and cluster support) a
+// 2048 points from global memory. With JMG_COARSE=cluster (and cluster support) a
 // thread-block cluster of 16 CTAs (8 where 16 is not allowed) takes every level from
 // the first one of at most 20 000 padded points whose rows, with the levels below, fit
 // in 200 KB of shared memory per CTA. On GB300 the coarse levels are bound by the
@@ -543,18 +546,18 @@ long long body_launches(const JmgPlan* p) {
   return n;
 }
 
-int build_graph(JmgPlan* p, void* ws) {
-  if (p->exec && p->exec_ws == ws) return JMG_OK;
-  if (p->exec) {
-    cudaGraphExecDestroy(p->exec);
-    p->exec = nullptr;
+int build_graph(JmgPlan* p, void* ws, cudaGraphExec_t* out) {
+  for (const JmgPlan::GraphSlot& g : p->graphs)
+    if (g.ws == ws) {
+      *out = g.exec;
+      return JMG_OK;
+    }
+  if ((int)p->graphs.size() >= JmgPlan::kMaxGraphs) {
+    // an exec still in flight is freed by the runtime once it completes
+    cudaGraphExecDestroy(p->graphs.front().exec);
+    p->graphs.erase(p->graphs.begin());
   }
   if (!p->cap) JMG_CUDA(cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking));
-  const int mode = loop_mode(p);
-  LoopState* st = ptr<LoopState>(ws, p->off_state);
-  double* parts = ptr<double>(ws, p->off_parts);
-  Lvl<double> l0 = lvl64(p, ws, 0);
-
   cudaGraph_t graph;
   JMG_CUDA(cudaGraphCreate(&graph, 0));
   cudaGraphConditionalHandle handle;
@@ -583,9 +586,8 @@ int build_graph(JmgPlan* p, void* ws) {
   cudaGraphExec_t exec;
   JMG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
   cudaGraphDestroy(graph);
-  p->exec = exec;
-  p->exec_ws = ws;
-  p->exec_mode = mode;
+  p->graphs.push_back({ws, exec});
+  *out = exec;
   return JMG_OK;
 }
 
@@ -740,8 +742,12 @@ int jmg_plan_create(JmgPlan** out, const JmgGrid* grid, const JmgConfig* cfg) {
 
 int jmg_plan_destroy(JmgPlan* p) {
   if (!p) return JMG_OK;
-  if (p->exec) cudaGraphExecDestroy(p->exec);
+  for (const JmgPlan::GraphSlot& g : p->graphs) cudaGraphExecDestroy(g.exec);
+  if (p->vjp_exec) cudaGraphExecDestroy(p->vjp_exec);
   if (p->cap) cudaStreamDestroy(p->cap);
+  for (cudaStream_t ls : p->lane_streams) cudaStreamDestroy(ls);
+  for (cudaEvent_t ev : p->lane_events) cudaEventDestroy(ev);
+  if (p->fork_event) cudaEventDestroy(p->fork_event);
   delete p;
   return JMG_OK;
 }
@@ -812,8 +818,9 @@ int jmg_solve(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs
   // 4. the loop
   const bool runs = p->cfg.max_iters_outer > 0;
   if (runs && !p->host_loop) {
-    if ((rc = build_graph(p, ws))) return rc;
-    JMG_CUDA(cudaGraphLaunch(p->exec, s));
+    cudaGraphExec_t exec = nullptr;
+    if ((rc = build_graph(p, ws, &exec))) return rc;
+    JMG_CUDA(cudaGraphLaunch(exec, s));
   } else if (runs) {
     emit_prologue(p, ws, 0, s);
     for (;;) {
@@ -851,7 +858,7 @@ static int solve_oneshot(int dim, const JmgGrid* grid, const JmgConfig* cfg, con
   int rc = jmg_plan_create(&p, grid, &cf);
   if (rc) return rc;
   rc = jmg_solve(p, phi0, rhs, c, phi_out, count_out, ws, bytes, stream);
-  if (rc == JMG_OK && p->exec) {
+  if (rc == JMG_OK && !p->graphs.empty()) {
     // the graph exec is destroyed with the plan: wait for the launch to finish first
     cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) rc = set_err(JMG_ERR_CUDA, "cudaStreamSynchronize failed: %s", cudaGetErrorString(e));

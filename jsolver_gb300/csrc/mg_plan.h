@@ -41,18 +41,31 @@ struct JmgPlan {
   bool fcg = false;
   size_t off_rho = 0, off_d = 0, off_q = 0, off_z64 = 0, off_fcg_parts = 0, off_tab64z = 0;
   int nparts = 0;
-  // graph cache
-  cudaGraphExec_t exec = nullptr;
-  void* exec_ws = nullptr;
-  int exec_mode = -1;
+  // graph cache: one executable graph per workspace address (a batched solve runs one
+  // workspace per lane, each with its own graph), oldest evicted beyond kMaxGraphs
+  struct GraphSlot {
+    void* ws;
+    cudaGraphExec_t exec;
+  };
+  static constexpr int kMaxGraphs = 32;
+  std::vector<GraphSlot> graphs;
   cudaStream_t cap = nullptr;
+  // batched solves: the lanes' streams and the events that fork them from and join them
+  // to the caller's stream
+  std::vector<cudaStream_t> lane_streams;
+  std::vector<cudaEvent_t> lane_events;
+  cudaEvent_t fork_event = nullptr;
+  // reverse mode: the checkpointed forward and the reverse sweep over the cycles, captured
+  // once per (workspace, adjoint workspace) address pair
+  cudaGraphExec_t vjp_exec = nullptr;
+  void *vjp_ws = nullptr, *vjp_aws = nullptr;
   // Host-driven loop instead of the conditional-WHILE graph (environment variable
   // JMG_HOST_LOOP=1 at plan creation): the same kernels, with the loop decision read back
   // after every iteration. Profilers cannot attribute kernel nodes inside graphs that hold
   // conditional nodes; this mode lets them see every launch.
   bool host_loop = false;
   // coarse sub-cycle on a thread-block cluster (cluster_ranks 0: the single-block
-  // global-memory kernel instead, from the first level of at most 8192 points)
+  // global-memory kernel instead, from the first level of at most 2048 points)
   int cluster_ranks = 0;
   bool coarse_ready = false;  // coarse_setup done
   bool force_block = true;    // single-block coarse kernel (JMG_COARSE=cluster at plan creation: cluster)

@@ -39,6 +39,23 @@ def solve_2d(grid_x, grid_y, phi, rhs, lam, D_xx, D_yy, *, D_xy=None, fixed=Fals
                          precision=precision, inner_cycles=inner_cycles, guess=guess, outer=outer)
 
 
+def solve_2d_batched(grid_x, grid_y, phi, rhs, lam, D_xx, D_yy, *, D_xy=None, lanes=8, fixed=False, epsilon=1e-12,
+                     gamma=1, fcycle=False, skip_pre=False, nu1=1, nu2=1, max_iters_outer=INT32_MAX,
+                     max_iters_inner=INT32_MAX, stop="distance", rtol=1e-10, precision="fp64", inner_cycles=1,
+                     outer="richardson"):
+    """B independent 2D solves in one call: jax.vmap(solve_2d) of the reference's
+    variational-inference use (README.md:107, examples/benchmark.py:1109-1230).
+
+    ``phi`` and ``rhs`` have shape (B, grid_y.mx + 3, grid_x.mx + 3); each coefficient
+    is a scalar, one array shared by the batch, or a (B, ...) array. Returns ``(phi,
+    counts)``, counts of length B; problem b's phi and count are solve_2d's on it alone.
+    ``lanes`` problems run concurrently (own workspace, stream and graph each)."""
+    return _engine.solve_batched((grid_x, grid_y), phi, rhs, lam, (D_xx, D_yy), D_xy, lanes=lanes, fixed=fixed,
+                                 epsilon=epsilon, gamma=gamma, fcycle=fcycle, skip_pre=skip_pre, nu1=nu1, nu2=nu2,
+                                 max_iters_outer=max_iters_outer, max_iters_inner=max_iters_inner, stop=stop,
+                                 rtol=rtol, precision=precision, inner_cycles=inner_cycles, outer=outer)
+
+
 globals().update(make_wrappers(2, solve_2d))
 
 

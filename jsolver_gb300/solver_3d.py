@@ -26,6 +26,19 @@ def solve_3d(grid_x, grid_y, grid_z, phi, rhs, lam, D_xx, D_yy, D_zz, *, fixed=F
                          precision=precision, inner_cycles=inner_cycles, outer=outer)
 
 
+def solve_3d_batched(grid_x, grid_y, grid_z, phi, rhs, lam, D_xx, D_yy, D_zz, *, lanes=8, fixed=False,
+                     epsilon=1e-12, gamma=1, fcycle=False, skip_pre=False, nu1=1, nu2=1, max_iters_outer=INT32_MAX,
+                     max_iters_inner=INT32_MAX, stop="distance", rtol=1e-10, precision="fp64", inner_cycles=1,
+                     outer="richardson"):
+    """B independent 3D solves in one call (jax.vmap(solve_3d)); arguments and results as
+    ``solver_2d.solve_2d_batched``, arrays of shape (B, grid_z.mx + 3, grid_y.mx + 3,
+    grid_x.mx + 3)."""
+    return _engine.solve_batched((grid_x, grid_y, grid_z), phi, rhs, lam, (D_xx, D_yy, D_zz), None, lanes=lanes,
+                                 fixed=fixed, epsilon=epsilon, gamma=gamma, fcycle=fcycle, skip_pre=skip_pre,
+                                 nu1=nu1, nu2=nu2, max_iters_outer=max_iters_outer, max_iters_inner=max_iters_inner,
+                                 stop=stop, rtol=rtol, precision=precision, inner_cycles=inner_cycles, outer=outer)
+
+
 globals().update(make_wrappers(3, solve_3d))
 
 

@@ -85,6 +85,30 @@ def test_shape_errors():
         s3.solve_3d_simple(g3, g3, g3, b, b, 0.0, b, b, 1.0)
 
 
+def test_batched_shape_errors_and_no_gpu(monkeypatch):
+    """Batched solves: (B, *spatial) phi/rhs, coefficients shared or (B, *spatial); the
+    per-problem rules are the single solve's; without a device the call raises."""
+    g = grid_1D(16)
+    a = np.zeros((3, 19, 19))
+    with pytest.raises(ValueError, match=r"batched phi and rhs must both have shape \(B, 19, 19\)"):
+        s2.solve_2d_batched(g, g, a[0], a[0], 0.0, 1.0, 1.0)
+    with pytest.raises(ValueError, match="batched phi and rhs"):
+        s2.solve_2d_batched(g, g, a, a[:2], 0.0, 1.0, 1.0)
+    with pytest.raises(ValueError, match="batch of 3"):
+        s2.solve_2d_batched(g, g, a, a, np.zeros((2, 19, 19)), 1.0, 1.0)
+    with pytest.raises(ValueError, match="Shape mismatch"):
+        s2.solve_2d_batched(g, g, a, a, 0.0, a[0], 1.0)  # D components mixed scalar/array
+    with pytest.raises(ValueError, match="dtype must be 'jnp.float64'"):
+        s2.solve_2d_batched(g, g, a.astype(np.float32), a, 0.0, 1.0, 1.0)
+    g3 = grid_1D(8)
+    b = np.zeros((2, 11, 11, 11))
+    with pytest.raises(ValueError, match="Shape mismatch.*D_zz="):
+        s3.solve_3d_batched(g3, g3, g3, b, b, 0.0, b, b, 1.0)
+    monkeypatch.setattr(torch.cuda, "is_available", lambda: False)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        s2.solve_2d_batched(g, g, a, a, 0.0, 1.0, 1.0)
+
+
 def test_no_gpu_fails_loudly(monkeypatch):
     """With valid arguments and no CUDA device the call raises; it never computes on the CPU."""
     monkeypatch.setattr(torch.cuda, "is_available", lambda: False)
@@ -95,8 +119,9 @@ def test_no_gpu_fails_loudly(monkeypatch):
 
 
 def test_wrappers_complete_and_positional():
-    names2 = sorted(n for n in dir(s2) if n.startswith("solve_2d_"))
-    names3 = sorted(n for n in dir(s3) if n.startswith("solve_3d_"))
+    # the reference's 18 wrappers per dimension; solve_*d_batched is this package's extension
+    names2 = sorted(n for n in dir(s2) if n.startswith("solve_2d_") and n != "solve_2d_batched")
+    names3 = sorted(n for n in dir(s3) if n.startswith("solve_3d_") and n != "solve_3d_batched")
     assert len(names2) == len(names3) == 18
     for suffix in ("", "_skip_pre", "_fcycle", "_fcycle_skip_pre", "_wcycle", "_wcycle_skip_pre"):
         assert list(inspect.signature(getattr(s2, f"solve_2d{suffix}_simple")).parameters)[:8] == \
