@@ -480,26 +480,30 @@ def main():
         err_exact = (float(np.abs(out.cpu().numpy() - p["phi_exact"]).max()) if "phi_exact" in p else None)
 
         # the fine-level red-black sweep of the form's cycles (FP64, or FP32 in the mixed
-        # forms; two colour launches), timed alone with CUDA events on its stream, L2
-        # flushed before every sweep
+        # forms; one launch per sweep where the level sweeps in one pass, else two colour
+        # launches), timed alone with CUDA events on its stream, L2 flushed before every
+        # timed interval. One-pass sweeps alternate two buffers, so they run in pairs.
         nsw = 20
         smooth = lib.jmg_op_smooth32_ws if precision == "mixed" else lib.jmg_op_smooth_ws
         elem = 4 if precision == "mixed" else 8
-        _lib.check(smooth(plan.handle, 0, 3, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()), vp(stream.cuda_stream)))
+        launches_per_sweep = lib.jmg_plan_sweep_launches(plan.handle, 0, 1 if precision == "mixed" else 0)
+        per = 2 if launches_per_sweep == 1 else 1
+        _lib.check(smooth(plan.handle, 0, 2 * per, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()),
+                          vp(stream.cuda_stream)))
         sw = []
         for _ in range(nsw):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            _lib.check(smooth(plan.handle, 0, 1, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()),
+            _lib.check(smooth(plan.handle, 0, per, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()),
                               vp(stream.cuda_stream)))
             e1.record(stream)
             sw.append((e0, e1))
         stream.synchronize()
-        sweep_ms = float(np.mean([a.elapsed_time(b) for a, b in sw]))
+        sweep_ms = float(np.mean([a.elapsed_time(b) for a, b in sw])) / per
         n0 = (m + 3) ** dim
         alg_bytes_sweep = (dim + 4) * elem * n0  # (d+4)*s*N0: phi, rhs, d faces, 1/A_cc read; phi written
-        launch_ms = sweep_ms / 2
+        launch_ms = sweep_ms / launches_per_sweep
         achieved = alg_bytes_sweep / (sweep_ms * 1e-3) / 1e9
 
         # end to end through the public API from pinned host buffers
@@ -549,7 +553,8 @@ def main():
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get(f"sweep_{'fp32' if elem == 4 else 'fp64'}_{dim}d_{m}")
+            traffic = json.load(f).get(f"sweep_{'fp32' if elem == 4 else 'fp64'}_{dim}d_{m}"
+                                       + ("_onepass" if launches_per_sweep == 1 else ""))
     except (OSError, ValueError):
         pass
 
@@ -571,11 +576,14 @@ def main():
         "guess_rel_residual": guess_rel_res,
         "max_err_vs_exact_discrete": err_exact,
         "roofline": {"bound": "hbm",
-                     "kernel": f"k_sweep_color{dim}d<{'float' if elem == 4 else 'double'}> (fine level; 2 launches "
-                               "per sweep)",
+                     "kernel": (f"k_sweep_fused3d<{'float' if elem == 4 else 'double'}> (fine level; one launch "
+                                "per sweep)" if launches_per_sweep == 1 else
+                                f"k_sweep_color{dim}d<{'float' if elem == 4 else 'double'}> (fine level; "
+                                f"{launches_per_sweep} launches per sweep)"),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src, "alg_bytes_per_sweep": alg_bytes_sweep,
-                     "alg_bytes_per_launch": alg_bytes_sweep / 2, "launch_ms": launch_ms, "traffic": traffic},
+                     "alg_bytes_per_launch": alg_bytes_sweep / launches_per_sweep, "launch_ms": launch_ms,
+                     "traffic": traffic},
         "e2e": ({"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
                 if e2e_ms is not None else None),
         "gpu_launches": int(launches),

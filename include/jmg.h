@@ -215,6 +215,11 @@ int jmg_op_smooth_ws(JmgPlan* plan, int level, int nsweeps, void* workspace, siz
 int jmg_op_smooth32_ws(JmgPlan* plan, int level, int nsweeps, void* workspace, size_t workspace_bytes,
                        jmg_stream_t stream);
 
+/* Kernel launches per sweep of a level in this plan's solves (fp32 != 0: the FP32
+ * cycles of a mixed plan): 1 for the one-pass 3D sweep, 2 colour passes, 4 sub-lattice
+ * passes with D_xy; 0 for a bad level. No reference counterpart. */
+int jmg_plan_sweep_launches(const JmgPlan* plan, int level, int fp32);
+
 /* Kernel launches of one jmg_solve: the fixed part (copies, hierarchy, loop set-up) and
  * the part repeated per loop iteration (one cycle plus its stopping test). No reference
  * counterpart: it reports this library's launch schedule. */

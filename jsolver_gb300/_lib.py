@@ -49,6 +49,7 @@ _SIGS = {
     "jmg_plan_levels": (ctypes.c_int, [_P]),
     "jmg_solve": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(JmgCoeffs), _P, _P, _P, ctypes.c_size_t, _P]),
     "jmg_batched_workspace_bytes": (ctypes.c_size_t, [_P, ctypes.c_int32]),
+    "jmg_plan_sweep_launches": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
     "jmg_solve_batched": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P, ctypes.POINTER(JmgCoeffs),
                                          ctypes.POINTER(JmgBatchStrides), _P, _P, _P, ctypes.c_size_t, _P]),
     "jmg_solve2d_f64": (ctypes.c_int, [ctypes.POINTER(JmgGrid), ctypes.POINTER(JmgConfig), _P, _P,

@@ -38,6 +38,9 @@ struct Lvl {
   int mx, my, mz;  // resolution per axis (interior indices 2..m)
   int P;           // row pitch in elements
   long long S;     // plane stride in elements (3D)
+  // second phi buffer of a level swept in one pass (launch_sweep_fused3d writes it and
+  // swaps the two); nullptr where the level uses the in-place colour passes
+  T* phi2;
 };
 
 constexpr int kMaxLevels = 16;

@@ -110,6 +110,20 @@ int validate_and_layout(JmgPlan* p) {
   if (p->cfg.off_diag && d != 2) return set_err(JMG_ERR_VALUE, "off_diag (D_xy) is a 2D option");
   p->off_diag = d == 2 && p->cfg.off_diag;
   p->lv.resize(p->used);
+  // one-pass sweeps (mg_fused.cu) for the 3D 7-point levels whose one-pass grid fills at
+  // least half a wave of the GPU (256^3 levels and finer), or, with
+  // JMG_FUSED_POINTS set, every level of at least that many padded points; these levels
+  // get a second phi buffer. FP32 levels by default, FP64 levels too with JMG_FUSED64=1;
+  // JMG_FUSED=0 turns them off.
+  const long long fused_min = [] {
+    const char* e = getenv("JMG_FUSED_POINTS");
+    const long long v = e ? atoll(e) : 0;
+    return v > 0 ? v : 0LL;
+  }();
+  const char* fe = getenv("JMG_FUSED");
+  const char* fe64 = getenv("JMG_FUSED64");
+  const bool fused_on = d == 3 && !(fe && fe[0] == '0');
+  const bool fused64 = fused_on && fe64 && fe64[0] == '1';
   size_t off = 0;
   auto take = [&](size_t bytes) {
     const size_t o = off;
@@ -137,7 +151,14 @@ int validate_and_layout(JmgPlan* p) {
     if (p->off_diag)
       for (int c = 0; c < 4; ++c) li.xd[c] = take(b8);
     for (int c = 0; c < 3; ++c) li.d[c] = (d == 3 && l >= 1) ? take(b8) : 0;
+    const bool fused_level =
+        fused_on && li.elems < (1ULL << 31) &&  // the one-pass kernel indexes with 32 bits
+        (fused_min > 0 ? (long long)li.elems >= fused_min
+                                   : fused_wave_permille(li.m[0], li.m[1], li.m[2]) >= 500);
+    li.phi2 = fused_level && fused64 ? take(b8) : 0;
+    li.phi2_32 = 0;
     if (p->mixed) {
+      if (fused_level) li.phi2_32 = take(b4);
       li.phi32 = take(b4);
       li.rhs32 = take(b4);
       li.wx32 = take(b4);
@@ -262,6 +283,7 @@ Lvl<double> jmg::lvl64(const JmgPlan* p, void* ws, int l) {
   a.wz = p->dim == 3 ? ptr<double>(ws, li.wz) : nullptr;
   a.invd = ptr<double>(ws, li.invd);
   a.acc = ptr<double>(ws, li.acc);
+  a.phi2 = li.phi2 ? ptr<double>(ws, li.phi2) : nullptr;
   a.mx = li.m[0];
   a.my = li.m[1];
   a.mz = li.m[2];
@@ -288,6 +310,7 @@ Lvl<float> jmg::lvl32(const JmgPlan* p, void* ws, int l) {
   a.wz = p->dim == 3 ? ptr<float>(ws, li.wz32) : nullptr;
   a.invd = ptr<float>(ws, li.invd32);
   a.acc = ptr<float>(ws, li.acc32);
+  a.phi2 = li.phi2_32 ? ptr<float>(ws, li.phi2_32) : nullptr;
   a.mx = li.m[0];
   a.my = li.m[1];
   a.mz = li.m[2];
@@ -343,9 +366,21 @@ void emit_cycle(const JmgPlan* p, LvlTable<T>& tab, const LvlTable<T>* dtab, con
                 bool fcycle, bool skip_pre, cudaStream_t s, long long* count = nullptr,
                 const EmitTop* top = nullptr) {
   const int dim = p->dim;
+  // One-pass sweeps write the level's second buffer and swap; an even number of them per
+  // visit leaves phi where the visit found it (the restriction, the prolongation and the
+  // caller's tables see the current buffer). An odd remainder runs as colour passes.
+  const int nsweeps = lev == cp.last_level ? cp.nu1 + cp.nu2 : (skip_pre ? 0 : cp.nu1) + cp.nu2;
+  int fused_left = tab.l[lev].phi2 ? nsweeps - nsweeps % 2 : 0;
   auto sweep = [&](bool first) {
-    if (count) *count += 2;  // two colour passes
-    else launch_sweep<T>(dim, tab.l[lev], s, top && top->zero_first && first);
+    const bool zero = top && top->zero_first && first;
+    if (fused_left > 0) {
+      --fused_left;
+      if (count) *count += 1;
+      else launch_sweep_fused3d<T>(tab.l[lev], zero, s);
+      return;
+    }
+    if (count) *count += dim == 2 && tab.l[lev].xll ? 4 : 2;  // colour (sub-lattice) passes
+    else launch_sweep<T>(dim, tab.l[lev], s, zero);
   };
   if (lev >= p->coarse_start) {
     if (count) *count += 1;
@@ -512,6 +547,10 @@ void emit_prologue(const JmgPlan* p, void* ws, unsigned long long handle, cudaSt
   launch_loop_init(st, parts, nparts, mode, p->cfg.rtol, p->cfg.max_iters_outer, handle, s);
 }
 
+// Counting emits no launch and reads no array: tables over this placeholder workspace
+// address only tell which arrays a level has (second phi buffers, D_xy couplings).
+void* const kCountBase = reinterpret_cast<void*>(static_cast<uintptr_t>(kAlign));
+
 long long body_launches(const JmgPlan* p) {
   long long n = 0;
   CycleParams cp = cycle_params(p, p->off_diag);
@@ -519,23 +558,19 @@ long long body_launches(const JmgPlan* p) {
     const int inner = p->cfg.inner_cycles > 0 ? p->cfg.inner_cycles : 1;
     const bool zero_first = p->coarse_start > 0 && p->cfg.nu1 >= 1;
     if (p->mixed) {
-      LvlTable<float> t;
-      memset(&t, 0, sizeof(t));
+      LvlTable<float> t = make_table<float>(p, kCountBase);
       for (int k = 0; k < inner; ++k) emit_cycle<float>(p, t, nullptr, cp, 0, p->cfg.fcycle != 0, false, nullptr, &n);
     } else {
-      LvlTable<double> t;
-      memset(&t, 0, sizeof(t));
+      LvlTable<double> t = make_table<double>(p, kCountBase);
       for (int k = 0; k < inner; ++k) emit_cycle<double>(p, t, nullptr, cp, 0, p->cfg.fcycle != 0, false, nullptr, &n);
     }
     return n + (p->mixed ? 4 : 3) + 1 + (zero_first ? 0 : 1);  // FCG update, loop step (+ memset node)
   }
   if (!p->mixed) {
-    LvlTable<double> t;
-    memset(&t, 0, sizeof(t));
+    LvlTable<double> t = make_table<double>(p, kCountBase);
     emit_cycle<double>(p, t, nullptr, cp, 0, p->cfg.fcycle != 0, p->cfg.skip_pre != 0, nullptr, &n);
   } else {
-    LvlTable<float> t;
-    memset(&t, 0, sizeof(t));
+    LvlTable<float> t = make_table<float>(p, kCountBase);
     const int inner = p->cfg.inner_cycles > 0 ? p->cfg.inner_cycles : 1;
     for (int k = 0; k < inner; ++k) emit_cycle<float>(p, t, nullptr, cp, 0, p->cfg.fcycle != 0, false, nullptr, &n);
     n += mixed_fused(p) ? 2 : (mixed_resid(p) ? 3 : 3 + (loop_mode(p) == 0));
@@ -704,6 +739,15 @@ bool jmg::pdl_enabled() {
 // C ABI
 // ---------------------------------------------------------------------------------------
 
+// nsweeps sweeps of one level as a solve runs them: one-pass sweeps in pairs where the
+// level has a second buffer (phi ends in the buffer it started in), colour passes else
+template <typename T>
+static void smooth_like_solve(const JmgPlan* p, Lvl<T>& a, int nsweeps, cudaStream_t s) {
+  const int fused = a.phi2 ? nsweeps - nsweeps % 2 : 0;
+  for (int k = 0; k < fused; ++k) launch_sweep_fused3d<T>(a, false, s);
+  for (int k = fused; k < nsweeps; ++k) launch_sweep<T>(p->dim, a, s);
+}
+
 extern "C" {
 
 void jmg_config_default(JmgConfig* c) {
@@ -796,6 +840,12 @@ int jmg_solve(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs
       tz.l[0].rhs = ptr<double>(ws, p->off_rho);
       launch_store_table<double>(tz, ptr<LvlTable<double>>(ws, p->off_tab64z), s);
     }
+  }
+  // second phi buffers: their frames must read zero (sweeps write interiors only)
+  for (int l = 0; l < p->used; ++l) {
+    const LevelInfo& li = p->lv[l];
+    if (li.phi2) JMG_CUDA(cudaMemsetAsync(ptr<char>(ws, li.phi2), 0, li.elems * 8, s));
+    if (li.phi2_32) JMG_CUDA(cudaMemsetAsync(ptr<char>(ws, li.phi2_32), 0, li.elems * 4, s));
   }
   if (p->mixed) {
     launch_store_table<float>(make_table<float>(p, ws), ptr<LvlTable<float>>(ws, p->off_tab32), s);
@@ -998,7 +1048,7 @@ int jmg_op_smooth_ws(JmgPlan* p, int level, int nsweeps, void* ws, size_t bytes,
   int rc = check_ws(p, ws, bytes);
   if (rc || (rc = level_check(p, level, false))) return rc;
   Lvl<double> a = lvl64(p, ws, level);
-  for (int k = 0; k < nsweeps; ++k) launch_sweep<double>(p->dim, a, (cudaStream_t)stream);
+  smooth_like_solve<double>(p, a, nsweeps, (cudaStream_t)stream);
   JMG_CUDA(cudaGetLastError());
   return JMG_OK;
 }
@@ -1008,9 +1058,16 @@ int jmg_op_smooth32_ws(JmgPlan* p, int level, int nsweeps, void* ws, size_t byte
   if (rc || (rc = level_check(p, level, false))) return rc;
   if (!p->mixed) return set_err(JMG_ERR_VALUE, "jmg_op_smooth32_ws needs a plan with precision mixed");
   Lvl<float> a = lvl32(p, ws, level);
-  for (int k = 0; k < nsweeps; ++k) launch_sweep<float>(p->dim, a, (cudaStream_t)stream);
+  smooth_like_solve<float>(p, a, nsweeps, (cudaStream_t)stream);
   JMG_CUDA(cudaGetLastError());
   return JMG_OK;
+}
+
+int jmg_plan_sweep_launches(const JmgPlan* p, int level, int fp32) {
+  if (!p || level < 0 || level >= p->used) return 0;
+  const LevelInfo& li = p->lv[level];
+  if (fp32 ? li.phi2_32 != 0 : li.phi2 != 0) return 1;
+  return p->off_diag ? 4 : 2;
 }
 
 const char* jmg_last_error(void) { return g_last_error.c_str(); }

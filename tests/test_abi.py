@@ -84,3 +84,32 @@ def test_launch_counts_follow_the_form():
         counts[name] = b.value
     # an FCG step adds its four vector kernels to the cycle and the stopping test
     assert counts["fcg"] >= counts["plain"] + 3
+
+
+def test_sweep_launches_per_level(monkeypatch):
+    """One-pass sweeps: 3D levels whose one-pass grid fills half a wave (256^3 and finer),
+    FP32 by default, FP64 with JMG_FUSED64=1, none with JMG_FUSED=0 or in 2D; each has a
+    second phi buffer. JMG_FUSED_POINTS selects levels by size instead."""
+    lib = _lib.load()
+    for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS"):
+        monkeypatch.delenv(k, raising=False)
+    g3 = _engine.make_grid((grid_1D(256),) * 3)
+    mixed = _engine.make_config(precision="mixed")
+    p = _lib.Plan(g3, mixed)
+    assert lib.jmg_plan_sweep_launches(p.handle, 0, 1) == 1   # 259^3 padded: one pass
+    assert lib.jmg_plan_sweep_launches(p.handle, 1, 1) == 2   # 131^3: colour passes
+    assert lib.jmg_plan_sweep_launches(p.handle, 0, 0) == 2   # FP64 levels: colour passes
+    assert lib.jmg_plan_sweep_launches(p.handle, 99, 1) == 0
+    monkeypatch.setenv("JMG_FUSED", "0")
+    off = _lib.Plan(g3, mixed)
+    assert lib.jmg_plan_sweep_launches(off.handle, 0, 1) == 2
+    assert off.workspace_bytes < p.workspace_bytes  # no second FP32 buffer
+    monkeypatch.delenv("JMG_FUSED")
+    monkeypatch.setenv("JMG_FUSED64", "1")
+    assert lib.jmg_plan_sweep_launches(_lib.Plan(g3, mixed).handle, 0, 0) == 1
+    monkeypatch.setenv("JMG_FUSED_POINTS", "100000")
+    small = _lib.Plan(_engine.make_grid((grid_1D(64),) * 3), mixed)
+    assert [lib.jmg_plan_sweep_launches(small.handle, lv, 1) for lv in range(3)] == [1, 2, 2]
+    g2 = _engine.make_grid((grid_1D(1024),) * 2)
+    assert lib.jmg_plan_sweep_launches(_lib.Plan(g2, mixed).handle, 0, 1) == 2
+    assert lib.jmg_plan_sweep_launches(_lib.Plan(g2, _engine.make_config(off_diag=True)).handle, 0, 0) == 4

@@ -1,0 +1,70 @@
+"""One-pass 3D sweeps (mg_fused.cu) against the two colour passes.
+
+The one-pass sweep computes every value with the colour passes' arithmetic in the same
+order, so whole solves must agree bit for bit with the one-pass sweep switched off
+(JMG_FUSED=0), for every cycle shape, sweep count and grid shape, in FP32 cycles and
+in FP64; the colour-pass solves are checked against the oracle in test_gpu_parity.py.
+The environment switches are read when a plan is created, so every case builds new plans.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():  # pragma: no cover
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+from jsolver_gb300 import _engine  # noqa: E402
+from jsolver_gb300.grid_1d import grid_1D  # noqa: E402
+from jsolver_gb300.solver_3d import solve_3d  # noqa: E402
+
+DEV = torch.device("cuda", 0)
+
+
+def _problem(mx, my, mz, seed):
+    rng = np.random.default_rng(seed)
+    shp = (mz + 3, my + 3, mx + 3)
+
+    def field(scale):
+        a = rng.standard_normal(shp) * scale
+        a[:2], a[-1:], a[:, :2], a[:, -1:], a[:, :, :2], a[:, :, -1:] = 0, 0, 0, 0, 0, 0
+        return a
+
+    D = [np.exp(field(0.7)) for _ in range(3)]
+    lam = np.abs(field(3.0))
+    rhs = field(1.0)
+    return [torch.from_numpy(x).to(DEV) for x in [np.zeros(shp), rhs, lam] + D]
+
+
+def _solve(monkeypatch, env, grids, args, **opts):
+    for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS"):
+        monkeypatch.delenv(k, raising=False)
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    _engine.CACHE.plans.clear()
+    _engine.CACHE.ws.clear()
+    return solve_3d(*grids, *args, **opts)
+
+
+CASES = [
+    ((64, 64, 64), dict(precision="mixed", stop="residual", outer="fcg", inner_cycles=2, fcycle=True)),
+    ((64, 64, 64), dict(precision="mixed", stop="residual")),
+    ((64, 32, 128), dict(precision="mixed", stop="residual", outer="fcg")),
+    ((128, 64, 32), dict(precision="mixed", fixed=True, max_iters_outer=6, gamma=2)),
+    ((64, 64, 64), dict(precision="mixed", fixed=True, max_iters_outer=5, nu1=2, nu2=1)),
+    ((64, 64, 64), dict(precision="mixed", fixed=True, max_iters_outer=5, skip_pre=True)),
+    ((32, 64, 64), dict(fixed=True, max_iters_outer=4, fcycle=True)),
+    ((64, 64, 64), dict()),
+]
+
+
+@pytest.mark.parametrize("shape,opts", CASES)
+def test_one_pass_equals_colour_passes(monkeypatch, shape, opts):
+    grids = tuple(grid_1D(m) for m in shape)
+    args = _problem(*shape, seed=sum(shape))
+    ref, c_ref = _solve(monkeypatch, {"JMG_FUSED": "0"}, grids, args, **opts)
+    # every level of at least 4096 points sweeps in one pass, FP32 and FP64
+    got, c_got = _solve(monkeypatch, {"JMG_FUSED_POINTS": "4096", "JMG_FUSED64": "1"}, grids, args, **opts)
+    assert int(c_got) == int(c_ref)
+    assert torch.equal(got, ref)
