@@ -185,7 +185,8 @@ template void launch_residual_partials<double>(int, const Lvl<double>&, const do
 __device__ double reduce_parts_warp(const double* parts, int n) {
   // called by one full warp; fixed assignment of parts to lanes, fixed shuffle tree
   double v = 0.0;
-  for (int t = threadIdx.x; t < n; t += 32) v += parts[t];
+#pragma unroll 8
+  for (int t = threadIdx.x; t < n; t += 32) v += parts[t];  // unrolled: loads in flight together
   return warp_sum(v);
 }
 

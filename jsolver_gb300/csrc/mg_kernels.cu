@@ -9,6 +9,9 @@
 // The coarse levels (few thousand points) run inside one thread block: k_coarse_cycle
 // executes the reference's recursion (solver_2d.py:582-614) from a given level down to
 // level L-2 with __syncthreads between operators, so a whole V/W/F sub-cycle is one launch.
+#include <cstdlib>
+#include <cstring>
+
 #include "mg_common.cuh"
 #include "mg_kernels.h"
 
@@ -386,6 +389,13 @@ void launch_restrict(int dim, const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s) 
     dim3 b(32, 8), g(cdiv(c.mx + 3, 32), cdiv(c.my + 3, 8));
     launch_k(k_restrict2d<T>, g, b, 0, s, f, c);
   } else {
+    // the tiled form (mg_tile3d.cu) unless JMG_RESTRICT3D=grid asks for one thread per
+    // coarse point; both give the same bits
+    const char* e = getenv("JMG_RESTRICT3D");
+    if (!(e && std::strcmp(e, "grid") == 0)) {
+      launch_restrict_tile3d<T>(f, c, s);
+      return;
+    }
     dim3 b(32, 8, 1), g(cdiv(c.mx + 3, 32), cdiv(c.my + 3, 8), c.mz + 3);
     launch_k(k_restrict3d<T>, g, b, 0, s, f, c);
   }

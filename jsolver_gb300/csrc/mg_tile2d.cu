@@ -83,40 +83,89 @@ constexpr int kFR = kDR + 2, kFC = kDC + 2;                  // with the one-poi
 template <typename T>
 __global__ void __launch_bounds__(256) k_restrict_tile2d(Lvl<T> f, Lvl<T> c) {
   pdl_enter();
+  constexpr int NT = 256;
   __shared__ T Phi[kFR][kFC];
   __shared__ T Def[kDR][kDC];
   const int J0 = blockIdx.y * kCJ, I0 = blockIdx.x * kCI;
   const int fr0 = 2 * J0 - 2, fc0 = 2 * I0 - 2;  // fine index of Def[0][0]
   const int tid = threadIdx.x;
   const long long P = f.P;
-  for (int t = tid; t < kFR * kFC; t += blockDim.x) {
-    const int r = t / kFC, q = t % kFC;
-    const int i = fr0 - 1 + r, j = fc0 - 1 + q;
-    T v = T(0);
-    if (i >= 0 && j >= 0 && i <= f.my + 2 && j <= f.mx + 2) v = f.phi[i * P + j];
-    Phi[r][q] = v;
+  // Every thread issues all its loads of a phase before using them: on the small levels
+  // these kernels are latency-bound, and one load per loop iteration made each phase
+  // wait once per iteration.
+  constexpr int U1 = (kFR * kFC + NT - 1) / NT;
+  {
+    T v[U1];
+#pragma unroll
+    for (int u = 0; u < U1; ++u) {
+      const int t = tid + u * NT;
+      v[u] = T(0);
+      if (t < kFR * kFC) {
+        const int r = t / kFC, q = t - r * kFC;
+        const int i = fr0 - 1 + r, j = fc0 - 1 + q;
+        if (i >= 0 && j >= 0 && i <= f.my + 2 && j <= f.mx + 2) v[u] = f.phi[i * P + j];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U1; ++u) {
+      const int t = tid + u * NT;
+      if (t < kFR * kFC) (&Phi[0][0])[t] = v[u];
+    }
   }
   __syncthreads();
-  for (int t = tid; t < kDR * kDC; t += blockDim.x) {
-    const int r = t / kDC, q = t % kDC;
-    const int i = fr0 + r, j = fc0 + q;
-    T d = T(0);
-    if (((i + j) & 1) == 0 && i >= 2 && i <= f.my && j >= 2 && j <= f.mx) {
-      const long long p = i * P + j;
-      const int rr = r + 1, qq = q + 1;  // position in Phi
-      // same operation order as defect_point2d
-      d = f.acc[p] * Phi[rr][qq];
-      d = fma(-f.wx[p - 1], Phi[rr][qq - 1], d);
-      d = fma(-f.wx[p], Phi[rr][qq + 1], d);
-      d = fma(-f.wy[p - P], Phi[rr - 1][qq], d);
-      d = fma(-f.wy[p], Phi[rr + 1][qq], d);
-      d = d + f.rhs[p];
+  constexpr int XR = (kDC + 1) / 2;  // red candidates per footprint row
+  constexpr int NRED = kDR * XR;
+  constexpr int U2 = (NRED + NT - 1) / NT;
+  {
+    T ac[U2], wxm[U2], wxp[U2], wym[U2], wyp[U2], rh[U2];
+    int pos[U2];
+#pragma unroll
+    for (int u = 0; u < U2; ++u) {
+      const int t = tid + u * NT;
+      pos[u] = -1;
+      if (t < NRED) {
+        const int r = t / XR, xp = t - r * XR;
+        const int i = fr0 + r;
+        const int q = 2 * xp + ((i + fc0) & 1);  // j = fc0 + q has i + j even (red)
+        const int j = fc0 + q;
+        if (q < kDC && i >= 2 && i <= f.my && j >= 2 && j <= f.mx) {
+          const long long p = i * P + j;
+          pos[u] = r * kDC + q;
+          ac[u] = f.acc[p];
+          wxm[u] = f.wx[p - 1];
+          wxp[u] = f.wx[p];
+          wym[u] = f.wy[p - P];
+          wyp[u] = f.wy[p];
+          rh[u] = f.rhs[p];
+        }
+      }
     }
-    Def[r][q] = d;
+    // the non-red entries of Def are never read; the red ones outside the interior are 0
+#pragma unroll
+    for (int u = 0; u < U2; ++u) {
+      const int t = tid + u * NT;
+      if (t >= NRED) continue;
+      const int r = t / XR, xp = t - r * XR;
+      const int i = fr0 + r;
+      const int q = 2 * xp + ((i + fc0) & 1);
+      if (q >= kDC) continue;
+      T d = T(0);
+      if (pos[u] >= 0) {
+        const int rr = r + 1, qq = q + 1;  // position in Phi
+        // same operation order as defect_point2d
+        d = ac[u] * Phi[rr][qq];
+        d = fma(-wxm[u], Phi[rr][qq - 1], d);
+        d = fma(-wxp[u], Phi[rr][qq + 1], d);
+        d = fma(-wym[u], Phi[rr - 1][qq], d);
+        d = fma(-wyp[u], Phi[rr + 1][qq], d);
+        d = d + rh[u];
+      }
+      Def[r][q] = d;
+    }
   }
   __syncthreads();
   const long long Pc = c.P;
-  for (int t = tid; t < kCJ * kCI; t += blockDim.x) {
+  for (int t = tid; t < kCJ * kCI; t += NT) {
     const int J = J0 + t / kCI, I = I0 + t % kCI;
     if (J > c.my + 2 || I > c.mx + 2) continue;
     T v = T(0);

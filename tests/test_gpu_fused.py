@@ -1,4 +1,5 @@
-"""One-pass 3D sweeps (mg_fused.cu) against the two colour passes.
+"""One-pass 3D sweeps (mg_fused.cu) and the tiled 3D restriction (mg_tile3d.cu) against
+the two colour passes and the one-thread-per-coarse-point restriction.
 
 The one-pass sweep computes every value with the colour passes' arithmetic in the same
 order, so whole solves must agree bit for bit with the one-pass sweep switched off
@@ -38,7 +39,7 @@ def _problem(mx, my, mz, seed):
 
 
 def _solve(monkeypatch, env, grids, args, **opts):
-    for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS"):
+    for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_RESTRICT3D"):
         monkeypatch.delenv(k, raising=False)
     for k, v in env.items():
         monkeypatch.setenv(k, v)
@@ -66,5 +67,16 @@ def test_one_pass_equals_colour_passes(monkeypatch, shape, opts):
     ref, c_ref = _solve(monkeypatch, {"JMG_FUSED": "0"}, grids, args, **opts)
     # every level of at least 4096 points sweeps in one pass, FP32 and FP64
     got, c_got = _solve(monkeypatch, {"JMG_FUSED_POINTS": "4096", "JMG_FUSED64": "1"}, grids, args, **opts)
+    assert int(c_got) == int(c_ref)
+    assert torch.equal(got, ref)
+
+
+@pytest.mark.parametrize("shape,opts", [CASES[0], CASES[2], CASES[6], CASES[7]])
+def test_tiled_restriction_equals_grid_restriction(monkeypatch, shape, opts):
+    """The same solves with the tiled 3D restriction (default) and the grid-wide one."""
+    grids = tuple(grid_1D(m) for m in shape)
+    args = _problem(*shape, seed=7 + sum(shape))
+    ref, c_ref = _solve(monkeypatch, {"JMG_RESTRICT3D": "grid"}, grids, args, **opts)
+    got, c_got = _solve(monkeypatch, {}, grids, args, **opts)
     assert int(c_got) == int(c_ref)
     assert torch.equal(got, ref)
