@@ -301,6 +301,8 @@ __global__ void __launch_bounds__(1024) k_coarse_smem32(const LvlTable<float>* t
     }
   }
   __syncthreads();
+  // copy-in: every thread issues four 16-byte loads before it stores them, so a level's
+  // arrays arrive in a few L2 round trips rather than one per loop iteration
   for (int l = lev0; l <= cp.last_level; ++l) {
     const Lvl<float>& g = tab->l[l];
     const Lvl<float>& v = st.l[l];
@@ -308,10 +310,24 @@ __global__ void __launch_bounds__(1024) k_coarse_smem32(const LvlTable<float>* t
     const float* src[6] = {g.phi, g.rhs, g.wx, g.wy, g.acc, g.invd};
     float* dst[6] = {v.phi, v.rhs, v.wx, v.wy, v.acc, v.invd};
     for (int a = l == lev0 ? 0 : 2; a < 6; ++a)
-      for (int t = threadIdx.x; t < n; t += blockDim.x) {
-        const int j = t / cpr, e = (t - j * cpr) * 4;
-        *reinterpret_cast<float4*>(dst[a] + j * v.P + e) =
-            __ldcg(reinterpret_cast<const float4*>(src[a] + (long long)j * g.P + e));
+      for (int t0 = threadIdx.x; t0 < n; t0 += 4 * blockDim.x) {
+        float4 w[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int t = t0 + u * blockDim.x;
+          if (t < n) {
+            const int j = t / cpr, e = (t - j * cpr) * 4;
+            w[u] = __ldcg(reinterpret_cast<const float4*>(src[a] + (long long)j * g.P + e));
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int t = t0 + u * blockDim.x;
+          if (t < n) {
+            const int j = t / cpr, e = (t - j * cpr) * 4;
+            *reinterpret_cast<float4*>(dst[a] + j * v.P + e) = w[u];
+          }
+        }
       }
   }
   __syncthreads();

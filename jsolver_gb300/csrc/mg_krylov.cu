@@ -13,6 +13,8 @@
 // solve is bitwise reproducible. The stopping test reads ||rho||, the recurrence
 // residual; it tracks the true residual to FP64 rounding over the few dozen steps a solve
 // takes (checked against jmg_rel_residual in the tests).
+#include <cstdlib>
+
 #include "mg_common.cuh"
 #include "mg_kernels.h"
 
@@ -25,7 +27,16 @@ namespace {
 // the longer reductions. It depends on the problem size only, so for a given problem the
 // reduction order is fixed and solves are bitwise reproducible.
 constexpr int kBlocks = 1216;  // the most blocks (partials) any FCG kernel uses
-__host__ __device__ inline int fcg_blocks(int rows) { return rows > 4096 ? 1216 : 304; }
+inline int fcg_blocks(int rows) {
+  // JMG_FCG_BLOCKS (152 .. 1216) overrides the choice for tuning runs
+  static const int forced = [] {
+    const char* e = getenv("JMG_FCG_BLOCKS");
+    const int v = e ? atoi(e) : 0;
+    return v >= 152 && v <= 1216 ? v : 0;
+  }();
+  if (forced) return forced;
+  return rows > 4096 ? 1216 : 304;
+}
 constexpr int kThreads = 256;
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -228,19 +239,19 @@ __device__ __forceinline__ float apply_L32(const Lvl<float>& a, const float* z, 
   return -t;
 }
 
-// The mixed-precision FCG kernels walk rows in groups of consecutive rows (3D: 2 or 4): each thread takes the same x in every row of a group and issues the group's loads
+// The mixed-precision FCG kernels walk rows in groups of consecutive rows: each thread takes the same x in every row of a group and issues the group's loads
 // together, so that a thread has several rows' loads in flight instead of one point's.
 // (A 3D row of 255 points is one point per thread; with one row at a time the kernels
 // were latency-bound at a third to a half of the DRAM bandwidth.) The order of every
 // sum is still fixed by the problem size alone.
 // Group sizes: 4 rows for the streaming kernels (dots, x update); the stencil kernels
-// (direction, residual) take one row at a time: their loads per row already fill the
-// registers (two rows per group: 80 registers, three blocks per SM, and a direction step
-// of 322 instead of 186 us at 3D 256^3).
+// (direction, residual) take two rows in 2D and one in 3D, where the loads of one row
+// already fill the registers (two rows per group: 80 registers, three blocks per SM,
+// and a direction step of 322 instead of 186 us at 3D 256^3).
 template <int DIM>
-constexpr int kGroup = DIM == 3 ? 4 : 1;
+constexpr int kGroup = 4;
 template <int DIM>
-constexpr int kGroupStencil = 1;
+constexpr int kGroupStencil = DIM == 2 ? 2 : 1;
 
 // rows of group g: their bases (0 where the row does not exist)
 template <int DIM, int G>
