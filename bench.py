@@ -576,8 +576,9 @@ def main():
         "guess_rel_residual": guess_rel_res,
         "max_err_vs_exact_discrete": err_exact,
         "roofline": {"bound": "hbm",
-                     "kernel": (f"k_sweep_fused3d<{'float' if elem == 4 else 'double'}> (fine level; one launch "
-                                "per sweep)" if launches_per_sweep == 1 else
+                     "kernel": (f"{'k_sweep_fused3d' if dim == 3 else 'k_sweep_onepass2d'}"
+                                f"<{'float' if elem == 4 else 'double'}> (fine level; one launch per sweep)"
+                                if launches_per_sweep == 1 else
                                 f"k_sweep_color{dim}d<{'float' if elem == 4 else 'double'}> (fine level; "
                                 f"{launches_per_sweep} launches per sweep)"),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -110,11 +110,13 @@ int validate_and_layout(JmgPlan* p) {
   if (p->cfg.off_diag && d != 2) return set_err(JMG_ERR_VALUE, "off_diag (D_xy) is a 2D option");
   p->off_diag = d == 2 && p->cfg.off_diag;
   p->lv.resize(p->used);
-  // one-pass sweeps (mg_fused.cu) for the 3D 7-point levels whose one-pass grid fills at
-  // least half a wave of the GPU (256^3 levels and finer), or, with
-  // JMG_FUSED_POINTS set, every level of at least that many padded points; these levels
-  // get a second phi buffer. FP32 levels by default, FP64 levels too with JMG_FUSED64=1;
-  // JMG_FUSED=0 turns them off.
+  // one-pass sweeps (mg_fused.cu), 5- and 7-point stencils: the 3D levels whose one-pass
+  // grid fills at least half a wave of the GPU (256^3 levels and finer); with
+  // JMG_FUSED2D=1 also the 2D levels of at least 2^18 padded points (512^2 and finer:
+  // faster alone from a cold L2, but not inside a 2D solve, where the level stays in L2);
+  // with JMG_FUSED_POINTS set, every level of at least that many padded points. These
+  // levels get a second phi buffer. FP32 levels by default, FP64 levels too with
+  // JMG_FUSED64=1; JMG_FUSED=0 turns them off.
   const long long fused_min = [] {
     const char* e = getenv("JMG_FUSED_POINTS");
     const long long v = e ? atoll(e) : 0;
@@ -122,8 +124,10 @@ int validate_and_layout(JmgPlan* p) {
   }();
   const char* fe = getenv("JMG_FUSED");
   const char* fe64 = getenv("JMG_FUSED64");
-  const bool fused_on = d == 3 && !(fe && fe[0] == '0');
+  const bool fused_on = !p->off_diag && !(fe && fe[0] == '0');
   const bool fused64 = fused_on && fe64 && fe64[0] == '1';
+  const char* fe2 = getenv("JMG_FUSED2D");
+  const bool fused2d = fe2 && fe2[0] == '1';
   size_t off = 0;
   auto take = [&](size_t bytes) {
     const size_t o = off;
@@ -152,9 +156,10 @@ int validate_and_layout(JmgPlan* p) {
       for (int c = 0; c < 4; ++c) li.xd[c] = take(b8);
     for (int c = 0; c < 3; ++c) li.d[c] = (d == 3 && l >= 1) ? take(b8) : 0;
     const bool fused_level =
-        fused_on && li.elems < (1ULL << 31) &&  // the one-pass kernel indexes with 32 bits
+        fused_on && li.elems < (1ULL << 31) &&  // the one-pass kernels index with 32 bits
         (fused_min > 0 ? (long long)li.elems >= fused_min
-                                   : fused_wave_permille(li.m[0], li.m[1], li.m[2]) >= 500);
+                       : d == 3 ? fused_wave_permille(li.m[0], li.m[1], li.m[2]) >= 500
+                                : fused2d && (long long)li.elems >= (1LL << 18));
     li.phi2 = fused_level && fused64 ? take(b8) : 0;
     li.phi2_32 = 0;
     if (p->mixed) {
@@ -376,7 +381,7 @@ void emit_cycle(const JmgPlan* p, LvlTable<T>& tab, const LvlTable<T>* dtab, con
     if (fused_left > 0) {
       --fused_left;
       if (count) *count += 1;
-      else launch_sweep_fused3d<T>(tab.l[lev], zero, s);
+      else launch_sweep_onepass<T>(dim, tab.l[lev], zero, s);
       return;
     }
     if (count) *count += dim == 2 && tab.l[lev].xll ? 4 : 2;  // colour (sub-lattice) passes
@@ -744,7 +749,7 @@ bool jmg::pdl_enabled() {
 template <typename T>
 static void smooth_like_solve(const JmgPlan* p, Lvl<T>& a, int nsweeps, cudaStream_t s) {
   const int fused = a.phi2 ? nsweeps - nsweeps % 2 : 0;
-  for (int k = 0; k < fused; ++k) launch_sweep_fused3d<T>(a, false, s);
+  for (int k = 0; k < fused; ++k) launch_sweep_onepass<T>(p->dim, a, false, s);
   for (int k = fused; k < nsweeps; ++k) launch_sweep<T>(p->dim, a, s);
 }
 

@@ -1,4 +1,4 @@
-// mg_fused.cu — one-pass red-black sweep of a 3D level (both colours in one launch).
+// mg_fused.cu — one-pass red-black sweeps (both colours in one launch), 3D and 2D.
 //
 // The two colour passes of launch_sweep each stream every array of the level: the
 // colours interleave within every cache line, so a pass that updates half the points
@@ -190,7 +190,179 @@ void launch_sweep_fused3d(Lvl<T>& a, bool zero_in, cudaStream_t s) {
   a.phi2 = t;
 }
 
+// ---- 2D -------------------------------------------------------------------------------
+// A 2D level of 1024^2 stays in L2 during a solve, so a march in y would wait on every
+// row; one block instead takes a 64 x 16 tile whole: the old phi of the tile with a
+// two-point halo into shared memory, the red values of the tile and a one-point ring from
+// it, one barrier, then the black values of the tile. Each phase's global loads are
+// issued before their first use. Same bits as the colour passes (gs_point2d's order).
+namespace {
+
+constexpr int k2TX = 64, k2TY = 16;
+constexpr int k2PX = k2TX + 4, k2PY = k2TY + 4;  // old phi, x from i0-2, y from j0-2
+constexpr int k2RX = k2TX + 2, k2RY = k2TY + 2;  // red ring, x from i0-1, y from j0-1
+constexpr int k2Threads = 256;
+constexpr int k2Red = k2RX * k2RY / 2;           // 594 red points in the ring region
+constexpr int k2Blk = k2TX * k2TY / 2;           // 512 black points in the tile
+
+template <typename T>
+__global__ void __launch_bounds__(k2Threads) k_sweep_onepass2d(Lvl<T> a, T* __restrict__ out, int zero_in) {
+  pdl_enter();
+  __shared__ T Ph[k2PY][k2PX];
+  __shared__ T Rd[k2RY][k2RX];
+  const int i0 = 2 + k2TX * blockIdx.x, j0 = 2 + k2TY * blockIdx.y;
+  const int tid = threadIdx.x;
+  const int P = a.P;
+  const bool zin = zero_in != 0;
+  // 1. old phi with a two-point halo (zero outside the padded array; unused with zero_in)
+  constexpr int NPH = k2PX * k2PY, U1 = (NPH + k2Threads - 1) / k2Threads;
+  if (!zin) {
+    T v[U1];
+#pragma unroll
+    for (int u = 0; u < U1; ++u) {
+      const int t = tid + u * k2Threads;
+      v[u] = T(0);
+      if (t < NPH) {
+        const int r = t / k2PX, q = t - r * k2PX;
+        const int j = j0 - 2 + r, i = i0 - 2 + q;
+        if (j >= 0 && i >= 0 && j <= a.my + 2 && i <= a.mx + 2) v[u] = a.phi[(long long)j * P + i];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U1; ++u) {
+      const int t = tid + u * k2Threads;
+      if (t < NPH) (&Ph[0][0])[t] = v[u];
+    }
+  }
+  // coefficients of the thread's red points (ring region, i + j even)
+  constexpr int U2 = (k2Red + k2Threads - 1) / k2Threads;
+  T rwxm[U2], rwxp[U2], rwym[U2], rwyp[U2], rrh[U2], rinv[U2];
+  int rpos[U2];  // r * k2RX + x in the red slots, -1 where the point is not interior
+#pragma unroll
+  for (int u = 0; u < U2; ++u) {
+    const int t = tid + u * k2Threads;
+    rpos[u] = -2;  // -2: no point; -1: a ring point outside the interior (value 0)
+    if (t < k2Red) {
+      const int r = t / (k2RX / 2), xp = t - r * (k2RX / 2);
+      const int j = j0 - 1 + r;
+      const int x = 2 * xp + ((j + i0 - 1) & 1);  // i = i0 - 1 + x with i + j even
+      const int i = i0 - 1 + x;
+      rpos[u] = -(r * k2RX + x) - 3;  // encoded slot of an exterior point
+      if (j >= 2 && j <= a.my && i >= 2 && i <= a.mx) {
+        const long long p = (long long)j * P + i;
+        rpos[u] = r * k2RX + x;
+        rrh[u] = a.rhs[p];
+        rinv[u] = a.invd[p];
+        if (!zin) {
+          rwxm[u] = a.wx[p - 1];
+          rwxp[u] = a.wx[p];
+          rwym[u] = a.wy[p - P];
+          rwyp[u] = a.wy[p];
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // coefficients of the thread's black points of the tile, issued before the red values
+  constexpr int U3 = k2Blk / k2Threads;  // 2
+  T bwxm[U3], bwxp[U3], bwym[U3], bwyp[U3], brh[U3], binv[U3];
+  long long bp[U3];
+  int bj[U3], bi[U3];
+#pragma unroll
+  for (int u = 0; u < U3; ++u) {
+    const int t = tid + u * k2Threads;
+    const int r = t / (k2TX / 2), xp = t - r * (k2TX / 2);
+    const int j = j0 + r;
+    const int i = i0 + 2 * xp + ((j + i0 + 1) & 1);  // i + j odd
+    bj[u] = j;
+    bi[u] = i;
+    bp[u] = (long long)j * P + i;
+    if (j <= a.my && i <= a.mx) {
+      const long long p = bp[u];
+      bwxm[u] = a.wx[p - 1];
+      bwxp[u] = a.wx[p];
+      bwym[u] = a.wy[p - P];
+      bwyp[u] = a.wy[p];
+      brh[u] = a.rhs[p];
+      binv[u] = a.invd[p];
+    }
+  }
+  // 2. red values of the ring region (gs_point2d's order)
+#pragma unroll
+  for (int u = 0; u < U2; ++u) {
+    if (rpos[u] == -2) continue;
+    if (rpos[u] < 0) {  // exterior ring point: the frame stays zero
+      (&Rd[0][0])[-(rpos[u] + 3)] = T(0);
+      continue;
+    }
+    const int r = rpos[u] / k2RX, x = rpos[u] - r * k2RX;
+    T v;
+    if (zin) {
+      v = (T(0) - rrh[u]) * rinv[u];
+    } else {
+      const int pr = r + 1, px = x + 1;  // position in Ph
+      T s = rwyp[u] * Ph[pr + 1][px];
+      s = fma(rwym[u], Ph[pr - 1][px], s);
+      s = fma(rwxp[u], Ph[pr][px + 1], s);
+      s = fma(rwxm[u], Ph[pr][px - 1], s);
+      s = s - rrh[u];
+      v = s * rinv[u];
+    }
+    Rd[r][x] = v;
+  }
+  __syncthreads();
+  // 3. black values of the tile from the new red values; both colours of the tile out
+#pragma unroll
+  for (int u = 0; u < U3; ++u) {
+    const int j = bj[u], i = bi[u];
+    if (j > a.my) continue;
+    const int r = j - (j0 - 1), x = i - (i0 - 1);  // position in Rd
+    if (i <= a.mx) {
+      T s = bwyp[u] * Rd[r + 1][x];
+      s = fma(bwym[u], Rd[r - 1][x], s);
+      s = fma(bwxp[u], Rd[r][x + 1], s);
+      s = fma(bwxm[u], Rd[r][x - 1], s);
+      s = s - brh[u];
+      out[bp[u]] = s * binv[u];
+    }
+  }
+  // red values of the tile
+  for (int t = tid; t < k2Blk; t += k2Threads) {
+    const int r = t / (k2TX / 2), xp = t - r * (k2TX / 2);
+    const int j = j0 + r;
+    const int i = i0 + 2 * xp + ((j + i0) & 1);  // i + j even
+    if (j <= a.my && i <= a.mx) out[(long long)j * P + i] = Rd[j - (j0 - 1)][i - (i0 - 1)];
+  }
+}
+
+}  // namespace
+
+template <typename T>
+void launch_sweep_onepass2d(Lvl<T>& a, bool zero_in, cudaStream_t s) {
+  dim3 g((a.mx - 1 + k2TX - 1) / k2TX, (a.my - 1 + k2TY - 1) / k2TY);
+  launch_k(k_sweep_onepass2d<T>, g, dim3(k2Threads), 0, s, a, a.phi2, zero_in ? 1 : 0);
+  T* t = a.phi;
+  a.phi = a.phi2;
+  a.phi2 = t;
+}
+
+template void launch_sweep_onepass2d<double>(Lvl<double>&, bool, cudaStream_t);
+template void launch_sweep_onepass2d<float>(Lvl<float>&, bool, cudaStream_t);
+
 template void launch_sweep_fused3d<double>(Lvl<double>&, bool, cudaStream_t);
 template void launch_sweep_fused3d<float>(Lvl<float>&, bool, cudaStream_t);
+
+}  // namespace jmg
+
+namespace jmg {
+
+template <typename T>
+void launch_sweep_onepass(int dim, Lvl<T>& a, bool zero_in, cudaStream_t s) {
+  if (dim == 3) launch_sweep_fused3d<T>(a, zero_in, s);
+  else launch_sweep_onepass2d<T>(a, zero_in, s);
+}
+
+template void launch_sweep_onepass<double>(int, Lvl<double>&, bool, cudaStream_t);
+template void launch_sweep_onepass<float>(int, Lvl<float>&, bool, cudaStream_t);
 
 }  // namespace jmg

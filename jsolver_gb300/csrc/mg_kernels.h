@@ -47,6 +47,10 @@ template <typename T> void launch_sweep(int dim, Lvl<T>& a, cudaStream_t s, bool
 // One-pass red-black sweep of a 3D level from a.phi into a.phi2, then the two pointers
 // swap (mg_fused.cu); bit-identical to launch_sweep. zero_in: phi is taken as zero.
 template <typename T> void launch_sweep_fused3d(Lvl<T>& a, bool zero_in, cudaStream_t s);
+// The 2D one-pass sweep (tiles of 64 x 16 with a halo, mg_fused.cu), and the dispatch of
+// either by dimension; levels with a second phi buffer only, no D_xy.
+template <typename T> void launch_sweep_onepass2d(Lvl<T>& a, bool zero_in, cudaStream_t s);
+template <typename T> void launch_sweep_onepass(int dim, Lvl<T>& a, bool zero_in, cudaStream_t s);
 template <typename T> void launch_restrict_tile3d(const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s);
 int fused_chunk3d(int mx, int my, int mz);
 int fused_blocks3d(int mx, int my, int mz);

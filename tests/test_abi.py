@@ -72,7 +72,8 @@ def test_config_extensions_are_validated_without_gpu():
     assert dxy >= base + 4 * n0  # four diagonal couplings per level
 
 
-def test_launch_counts_follow_the_form():
+def test_launch_counts_follow_the_form(monkeypatch):
+    monkeypatch.setenv("JMG_FUSED", "0")  # the same sweeps in both forms
     lib = _lib.load()
     g = _engine.make_grid((grid_1D(1024), grid_1D(1024)))
     counts = {}
@@ -88,10 +89,11 @@ def test_launch_counts_follow_the_form():
 
 def test_sweep_launches_per_level(monkeypatch):
     """One-pass sweeps: 3D levels whose one-pass grid fills half a wave (256^3 and finer),
-    FP32 by default, FP64 with JMG_FUSED64=1, none with JMG_FUSED=0 or in 2D; each has a
-    second phi buffer. JMG_FUSED_POINTS selects levels by size instead."""
+    2D levels of at least 2^18 padded points with JMG_FUSED2D=1, FP32 by default, FP64
+    with JMG_FUSED64=1, none with JMG_FUSED=0 or with D_xy; each has a second phi buffer.
+    JMG_FUSED_POINTS selects levels by size instead."""
     lib = _lib.load()
-    for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS"):
+    for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_FUSED2D"):
         monkeypatch.delenv(k, raising=False)
     g3 = _engine.make_grid((grid_1D(256),) * 3)
     mixed = _engine.make_config(precision="mixed")
@@ -110,6 +112,11 @@ def test_sweep_launches_per_level(monkeypatch):
     monkeypatch.setenv("JMG_FUSED_POINTS", "100000")
     small = _lib.Plan(_engine.make_grid((grid_1D(64),) * 3), mixed)
     assert [lib.jmg_plan_sweep_launches(small.handle, lv, 1) for lv in range(3)] == [1, 2, 2]
+    monkeypatch.delenv("JMG_FUSED_POINTS")
     g2 = _engine.make_grid((grid_1D(1024),) * 2)
-    assert lib.jmg_plan_sweep_launches(_lib.Plan(g2, mixed).handle, 0, 1) == 2
+    assert [lib.jmg_plan_sweep_launches(_lib.Plan(g2, mixed).handle, lv, 1) for lv in range(3)] == [2, 2, 2]
+    monkeypatch.setenv("JMG_FUSED2D", "1")
+    p2 = _lib.Plan(g2, mixed)
+    # 2D opt-in: 1027 x 1040 and 515 x 528 padded points sweep in one pass, 259 x 272 in two
+    assert [lib.jmg_plan_sweep_launches(p2.handle, lv, 1) for lv in range(3)] == [1, 1, 2]
     assert lib.jmg_plan_sweep_launches(_lib.Plan(g2, _engine.make_config(off_diag=True)).handle, 0, 0) == 4

@@ -103,3 +103,19 @@ def test_batched_workspace_lanes_and_errors():
         solve_2d_batched(g, g, torch.zeros(2, 19, 19, dtype=torch.float64, device=DEV),
                          torch.zeros(2, 19, 19, dtype=torch.float64, device=DEV),
                          torch.zeros(3, 19, 19, dtype=torch.float64, device=DEV), 1.0, 1.0)
+
+
+def test_batched_dxy_and_w_cycles():
+    """The 9-point stencil (D_xy batched per problem) and W-cycles through the batched call."""
+    m, nb = 32, 3
+    g = grid_1D(m)
+    rng = np.random.default_rng(5)
+    probs = [W.random_2d(m, seed=60 + b) for b in range(nb)]
+    dxy = np.stack([0.3 * np.minimum(p["D_xx"], p["D_yy"]) * rng.uniform(-1, 1, p["D_xx"].shape) for p in probs])
+    X = [_stack(probs, k) for k in ("phi0", "rhs", "lam", "D_xx", "D_yy")]
+    Dxy = torch.from_numpy(dxy).to(DEV)
+    for opts in (dict(fixed=True, max_iters_outer=6), dict(gamma=2, stop="residual", precision="mixed", outer="fcg")):
+        phi, cnt = solve_2d_batched(g, g, *X, D_xy=Dxy, lanes=2, **opts)
+        for b in range(nb):
+            one, c1 = solve_2d(g, g, *[x[b] for x in X], D_xy=Dxy[b], **opts)
+            assert torch.equal(phi[b], one) and int(cnt[b]) == int(c1), (opts, b)

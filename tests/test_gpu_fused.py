@@ -1,5 +1,5 @@
-"""One-pass 3D sweeps (mg_fused.cu) and the tiled 3D restriction (mg_tile3d.cu) against
-the two colour passes and the one-thread-per-coarse-point restriction.
+"""One-pass sweeps (mg_fused.cu, 3D and 2D) and the tiled 3D restriction (mg_tile3d.cu)
+against the two colour passes and the one-thread-per-coarse-point restriction.
 
 The one-pass sweep computes every value with the colour passes' arithmetic in the same
 order, so whole solves must agree bit for bit with the one-pass sweep switched off
@@ -39,7 +39,7 @@ def _problem(mx, my, mz, seed):
 
 
 def _solve(monkeypatch, env, grids, args, **opts):
-    for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_RESTRICT3D"):
+    for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_RESTRICT3D", "JMG_FUSED2D"):
         monkeypatch.delenv(k, raising=False)
     for k, v in env.items():
         monkeypatch.setenv(k, v)
@@ -78,5 +78,44 @@ def test_tiled_restriction_equals_grid_restriction(monkeypatch, shape, opts):
     args = _problem(*shape, seed=7 + sum(shape))
     ref, c_ref = _solve(monkeypatch, {"JMG_RESTRICT3D": "grid"}, grids, args, **opts)
     got, c_got = _solve(monkeypatch, {}, grids, args, **opts)
+    assert int(c_got) == int(c_ref)
+    assert torch.equal(got, ref)
+
+
+CASES_2D = [
+    ((256, 256), dict(precision="mixed", stop="residual", outer="fcg", inner_cycles=2)),
+    ((256, 256), dict(precision="mixed", stop="residual")),
+    ((128, 256), dict(precision="mixed", fixed=True, max_iters_outer=6, gamma=2)),
+    ((256, 128), dict(fixed=True, max_iters_outer=5, nu1=2, nu2=1)),
+    ((256, 256), dict(fixed=True, max_iters_outer=5, skip_pre=True, fcycle=True)),
+    ((256, 256), dict()),
+]
+
+
+@pytest.mark.parametrize("shape,opts", CASES_2D)
+def test_one_pass_2d_equals_colour_passes(monkeypatch, shape, opts):
+    from jsolver_gb300 import workloads as W
+    from jsolver_gb300.solver_2d import solve_2d
+    mx, my = shape
+    p = W.random_2d(max(mx, my), seed=mx + 3 * my)
+    sl = (slice(0, my + 3), slice(0, mx + 3))
+    args = [torch.from_numpy(np.ascontiguousarray(p[k][sl])).to(DEV) for k in ("phi0", "rhs", "lam", "D_xx", "D_yy")]
+    args[1] = args[1].clone()
+    args[1][-1:, :] = 0  # a frame of zeros where the slice cut the field
+    args[1][:, -1:] = 0
+    grids = (grid_1D(mx), grid_1D(my))
+
+    def run(env):
+        for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_RESTRICT3D", "JMG_FUSED2D"):
+            monkeypatch.delenv(k, raising=False)
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        _engine.CACHE.plans.clear()
+        _engine.CACHE.ws.clear()
+        return solve_2d(*grids, *args, **opts)
+
+    ref, c_ref = run({"JMG_FUSED": "0"})
+    # every level of at least 1000 points sweeps in one pass, FP32 and FP64
+    got, c_got = run({"JMG_FUSED_POINTS": "1000", "JMG_FUSED64": "1"})
     assert int(c_got) == int(c_ref)
     assert torch.equal(got, ref)
