@@ -252,11 +252,22 @@ __device__ void blk_cycle(const LvlTable<T>* __restrict__ tab, const CycleParams
   }
 }
 
+// The level table (~2 KB) is copied into shared memory first: every frame of the cycle
+// reads its level's pointers and sizes, and from the global table each of those reads
+// was an L2 round trip in front of the frame's first pass.
 template <typename T, int DIM>
 __global__ void __launch_bounds__(1024) k_coarse_cycle(const LvlTable<T>* tab, CycleParams cp, int lev, int fcycle,
                                                       int skip_pre) {
   pdl_enter();
-  blk_cycle<T, DIM>(tab, cp, lev, fcycle != 0, skip_pre != 0);
+  __shared__ LvlTable<T> stab;
+  {
+    const int n = (int)(sizeof(LvlTable<T>) / sizeof(int));
+    const int* src = reinterpret_cast<const int*>(tab);
+    int* dst = reinterpret_cast<int*>(&stab);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) dst[k] = src[k];
+  }
+  __syncthreads();
+  blk_cycle<T, DIM>(&stab, cp, lev, fcycle != 0, skip_pre != 0);
 }
 
 // FP32 2D coarse sub-cycle from shared memory. Every array of levels lev0 .. last (phi,

@@ -129,6 +129,38 @@ __device__ __forceinline__ double apply_L(const Lvl<double>& a, const TZ* z, lon
   return -t;
 }
 
+// The streaming FCG kernels walk rows in groups of consecutive rows: each thread takes the same x in every row of a group and issues the group's loads
+// together, so that a thread has several rows' loads in flight instead of one point's.
+// (A 3D row of 255 points is one point per thread; with one row at a time the kernels
+// were latency-bound at a third to a half of the DRAM bandwidth.) The order of every
+// sum is still fixed by the problem size alone.
+// Group sizes: 4 rows for the streaming kernels (dots, x update); the stencil kernels
+// (direction, residual) take two rows in 2D and one in 3D, where the loads of one row
+// already fill the registers (two rows per group: 80 registers, three blocks per SM,
+// and a direction step of 322 instead of 186 us at 3D 256^3).
+template <int DIM>
+constexpr int kGroup = 4;
+template <int DIM>
+constexpr int kGroupStencil = DIM == 2 ? 2 : 1;
+
+// rows of group g: their bases (0 where the row does not exist)
+template <int DIM, int G>
+__device__ __forceinline__ int group_rows(const Lvl<double>& a, int g, int nr, long long* base) {
+  int n = 0;
+#pragma unroll
+  for (int u = 0; u < G; ++u) {
+    const int r = g * G + u;
+    base[u] = r < nr ? row_base<DIM>(a, r) : 0;
+    n += r < nr;
+  }
+  return n;
+}
+
+#define JMG_FOR_GROUPS(a, G)                                                                 \
+  for (int g_ = blockIdx.x, nr_ = nrows<DIM>(a); g_ * (G) < nr_; g_ += gridDim.x)           \
+    for (long long base_[G], n_ = group_rows<DIM, G>(a, g_, nr_, base_), i_ = 2 + threadIdx.x; \
+         i_ <= (a).mx; i_ += kThreads)
+
 // rho = rhs - L x, d = q = 0, r32 = float(rho); partials of rho . rho
 template <int DIM>
 __global__ void __launch_bounds__(kThreads) k_fcg_init(Lvl<double> a, double* rho, double* d, double* q, float* r32,
@@ -150,14 +182,27 @@ __global__ void __launch_bounds__(kThreads) k_fcg_init(Lvl<double> a, double* rh
 
 // partials of z . q and d . q (the previous direction)
 template <int DIM, typename TZ>
-__global__ void __launch_bounds__(kThreads) k_fcg_dots(Lvl<double> a, const TZ* z, const double* d, const double* q,
+__global__ void __launch_bounds__(kThreads) k_fcg_dots(Lvl<double> a, const TZ* __restrict__ z,
+                                                      const double* __restrict__ d, const double* __restrict__ q,
                                                       double* parts) {
   pdl_enter();
   double zq = 0.0, dq = 0.0;
-  JMG_FOR_POINTS(a, p) {
-    const double qp = q[p];
-    zq = fma((double)z[p], qp, zq);
-    dq = fma(d[p], qp, dq);
+  JMG_FOR_GROUPS(a, kGroup<DIM>) {
+    double zv[kGroup<DIM>], dv[kGroup<DIM>], qv[kGroup<DIM>];
+#pragma unroll
+    for (int u = 0; u < kGroup<DIM>; ++u)
+      if (u < n_) {
+        const long long p = base_[u] + i_;
+        zv[u] = (double)z[p];
+        dv[u] = d[p];
+        qv[u] = q[p];
+      }
+#pragma unroll
+    for (int u = 0; u < kGroup<DIM>; ++u)
+      if (u < n_) {
+        zq = fma(zv[u], qv[u], zq);
+        dq = fma(dv[u], qv[u], dq);
+      }
   }
   block_sum2(zq, dq);
   if (threadIdx.x == 0) {
@@ -192,19 +237,36 @@ __global__ void __launch_bounds__(kThreads) k_fcg_dir(Lvl<double> a, const TZ* z
 
 // alpha from the dots; x += alpha d, rho -= alpha q, r32 = float(rho); partials of rho . rho
 template <int DIM>
-__global__ void __launch_bounds__(kThreads) k_fcg_step(Lvl<double> a, const double* d, const double* q, double* rho,
-                                                      float* r32, const double* parts_in, double* parts) {
+__global__ void __launch_bounds__(kThreads) k_fcg_step(Lvl<double> a, const double* __restrict__ d,
+                                                      const double* __restrict__ q, double* __restrict__ rho,
+                                                      float* __restrict__ r32, const double* parts_in, double* parts) {
   pdl_enter();
   double dr, dq;
   totals2(parts_in, &dr, &dq);
   const double alpha = dq != 0.0 ? dr / dq : 0.0;
   double s = 0.0, unused = 0.0;
-  JMG_FOR_POINTS(a, p) {
-    a.phi[p] = fma(alpha, d[p], a.phi[p]);
-    const double r = fma(-alpha, q[p], rho[p]);
-    rho[p] = r;
-    if (r32) r32[p] = (float)r;
-    s = fma(r, r, s);
+  double* __restrict__ x = a.phi;
+  JMG_FOR_GROUPS(a, kGroup<DIM>) {
+    double xv[kGroup<DIM>], dv[kGroup<DIM>], qv[kGroup<DIM>], rv[kGroup<DIM>];
+#pragma unroll
+    for (int u = 0; u < kGroup<DIM>; ++u)
+      if (u < n_) {
+        const long long p = base_[u] + i_;
+        xv[u] = x[p];
+        dv[u] = d[p];
+        qv[u] = q[p];
+        rv[u] = rho[p];
+      }
+#pragma unroll
+    for (int u = 0; u < kGroup<DIM>; ++u)
+      if (u < n_) {
+        const long long p = base_[u] + i_;
+        x[p] = fma(alpha, dv[u], xv[u]);
+        const double r = fma(-alpha, qv[u], rv[u]);
+        rho[p] = r;
+        if (r32) r32[p] = (float)r;
+        s = fma(r, r, s);
+      }
   }
   block_sum2(s, unused);
   if (threadIdx.x == 0) parts[blockIdx.x] = s;
@@ -238,38 +300,6 @@ __device__ __forceinline__ float apply_L32(const Lvl<float>& a, const float* z, 
   }
   return -t;
 }
-
-// The mixed-precision FCG kernels walk rows in groups of consecutive rows: each thread takes the same x in every row of a group and issues the group's loads
-// together, so that a thread has several rows' loads in flight instead of one point's.
-// (A 3D row of 255 points is one point per thread; with one row at a time the kernels
-// were latency-bound at a third to a half of the DRAM bandwidth.) The order of every
-// sum is still fixed by the problem size alone.
-// Group sizes: 4 rows for the streaming kernels (dots, x update); the stencil kernels
-// (direction, residual) take two rows in 2D and one in 3D, where the loads of one row
-// already fill the registers (two rows per group: 80 registers, three blocks per SM,
-// and a direction step of 322 instead of 186 us at 3D 256^3).
-template <int DIM>
-constexpr int kGroup = 4;
-template <int DIM>
-constexpr int kGroupStencil = DIM == 2 ? 2 : 1;
-
-// rows of group g: their bases (0 where the row does not exist)
-template <int DIM, int G>
-__device__ __forceinline__ int group_rows(const Lvl<double>& a, int g, int nr, long long* base) {
-  int n = 0;
-#pragma unroll
-  for (int u = 0; u < G; ++u) {
-    const int r = g * G + u;
-    base[u] = r < nr ? row_base<DIM>(a, r) : 0;
-    n += r < nr;
-  }
-  return n;
-}
-
-#define JMG_FOR_GROUPS(a, G)                                                                 \
-  for (int g_ = blockIdx.x, nr_ = nrows<DIM>(a); g_ * (G) < nr_; g_ += gridDim.x)           \
-    for (long long base_[G], n_ = group_rows<DIM, G>(a, g_, nr_, base_), i_ = 2 + threadIdx.x; \
-         i_ <= (a).mx; i_ += kThreads)
 
 // rho = rhs - L x (FP64), r32 = float(rho), d32 = q32 = 0; partials of rho . rho
 template <int DIM>
