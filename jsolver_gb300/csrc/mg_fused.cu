@@ -32,7 +32,12 @@ constexpr int kRY = kTY + 2;                 // y from j0-1 to j0+8
 constexpr int kRed = kRX * kRY / 2;          // red points of the ring region per plane (330)
 constexpr int kThreads = 384;                // one red point per thread and plane
 constexpr int kSlots = 4;                    // red planes k-1 .. k+2 live in one step
+// Four blocks per SM (40 registers). FP64 levels sweep in one pass only on request
+// (JMG_FUSED64=1): at four blocks per SM the FP64 form spills (375 us per 256^3 sweep),
+// at two it does not but hides less latency (451 us); the colour passes take 287 us.
 constexpr int kBlocksPerSM = 4;
+template <typename T>
+constexpr int kBlocksPerSMT = kBlocksPerSM;
 
 // Inputs of one red value, loaded ahead of their use so that their DRAM latency overlaps
 // the black update of an earlier plane; then the value, with gs_point3d's arithmetic.
@@ -69,7 +74,7 @@ __device__ __forceinline__ T red_eval(const RedIn<T>& r, bool zero_in) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads, kBlocksPerSM)
+__global__ void __launch_bounds__(kThreads, kBlocksPerSMT<T>)
     k_sweep_fused3d(Lvl<T> a, T* __restrict__ out, int zero_in, int kchunk) {
   pdl_enter();
   __shared__ T red[kSlots][kRY][kRX];
@@ -159,9 +164,9 @@ __global__ void __launch_bounds__(kThreads, kBlocksPerSM)
 // SMs): a partial second wave would run at a fraction of the occupancy for a whole
 // block's time. Chunks have at least 16 planes, so the three planes each chunk starts
 // with stay a small share.
-int fused_chunk3d(int mx, int my, int mz) {
+int fused_chunk3d(int mx, int my, int mz, int blocks_per_sm) {
   const long long tiles = (long long)((mx - 1 + kTX - 1) / kTX) * ((my - 1 + kTY - 1) / kTY);
-  const long long resident = 152LL * kBlocksPerSM;
+  const long long resident = 152LL * blocks_per_sm;
   const int planes = mz - 1;
   long long nchunk = resident / tiles;
   const long long maxchunk = (planes + 15) / 16;
@@ -171,7 +176,7 @@ int fused_chunk3d(int mx, int my, int mz) {
 }
 
 int fused_blocks3d(int mx, int my, int mz) {
-  const int kchunk = fused_chunk3d(mx, my, mz);
+  const int kchunk = fused_chunk3d(mx, my, mz, kBlocksPerSM);
   return ((mx - 1 + kTX - 1) / kTX) * ((my - 1 + kTY - 1) / kTY) * ((mz - 1 + kchunk - 1) / kchunk);
 }
 
@@ -182,7 +187,7 @@ int fused_wave_permille(int mx, int my, int mz) {
 
 template <typename T>
 void launch_sweep_fused3d(Lvl<T>& a, bool zero_in, cudaStream_t s) {
-  const int kchunk = fused_chunk3d(a.mx, a.my, a.mz);
+  const int kchunk = fused_chunk3d(a.mx, a.my, a.mz, kBlocksPerSMT<T>);
   dim3 g((a.mx - 1 + kTX - 1) / kTX, (a.my - 1 + kTY - 1) / kTY, (a.mz - 1 + kchunk - 1) / kchunk);
   launch_k(k_sweep_fused3d<T>, g, dim3(kThreads), 0, s, a, a.phi2, zero_in ? 1 : 0, kchunk);
   T* t = a.phi;
