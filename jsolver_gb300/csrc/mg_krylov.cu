@@ -22,10 +22,10 @@ namespace jmg {
 
 namespace {
 
-// Block count of the FCG kernels: 304 (2 per SM) for up to 4096 interior rows, 1216 (8
-// per SM) above, where the vectors are large enough for the extra parallelism to pay for
-// the longer reductions. It depends on the problem size only, so for a given problem the
-// reduction order is fixed and solves are bitwise reproducible.
+// Block count of the FCG kernels: 304 (2 per SM) for up to 4096 interior rows, 608 (4
+// per SM) above (3D 256^3 headline: 104.2 ms against 106.3 with 1216 and 119 with 304;
+// 2D 1024^2: 304 beats 608 and 1216). It depends on the problem size only, so for a
+// given problem the reduction order is fixed and solves are bitwise reproducible.
 constexpr int kBlocks = 1216;  // the most blocks (partials) any FCG kernel uses
 inline int fcg_blocks(int rows) {
   // JMG_FCG_BLOCKS (152 .. 1216) overrides the choice for tuning runs
@@ -35,7 +35,7 @@ inline int fcg_blocks(int rows) {
     return v >= 152 && v <= 1216 ? v : 0;
   }();
   if (forced) return forced;
-  return rows > 4096 ? 1216 : 304;
+  return rows > 4096 ? 608 : 304;
 }
 constexpr int kThreads = 256;
 
