@@ -434,6 +434,13 @@ void launch_prolong(int dim, const Lvl<T>& f, const Lvl<T>& c, int diag, cudaStr
     dim3 b(64, 4), g(cdiv(f.mx - 1, 64), cdiv(f.my - 1, 4));
     launch_k(k_prolong2d<T>, g, b, 0, s, f, c, diag);
   } else {
+    // by coarse cells (mg_tile3d.cu) unless JMG_PROLONG3D=grid asks for one thread per
+    // fine point; both give the same bits
+    const char* e = getenv("JMG_PROLONG3D");
+    if (!(e && std::strcmp(e, "grid") == 0)) {
+      launch_prolong_cells3d<T>(f, c, diag, s);
+      return;
+    }
     dim3 b(64, 4, 1), g(cdiv(f.mx - 1, 64), cdiv(f.my - 1, 4), f.mz - 1);
     launch_k(k_prolong3d<T>, g, b, 0, s, f, c, diag);
   }

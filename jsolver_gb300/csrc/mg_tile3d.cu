@@ -1,4 +1,5 @@
-// mg_tile3d.cu — 3D defect + restriction with every fine defect computed once.
+// mg_tile3d.cu — 3D defect + restriction with every fine defect computed once, and the
+// 3D prolongation by coarse cells.
 //
 // The coarse right-hand side at (K, J, I) is 1/32 of the defects at the 12 red fine
 // points around (2K-1, 2J-1, 2I-1) that differ from it in two coordinates by 1, plus 1/8
@@ -139,6 +140,65 @@ __global__ void __launch_bounds__(CK * CJ * CI) k_restrict_tile3d(Lvl<T> f, Lvl<
   }
 }
 
+// ---- prolongation --------------------------------------------------------------------
+// phi_f += P phi_c (solver_3d.py:654-677) by coarse cells: a thread takes the 2 x 2 x 2
+// fine points (2K-1 .. 2K, 2J-1 .. 2J, 2I-1 .. 2I), which all interpolate from the eight
+// coarse corners (K .. K+1, J .. J+1, I .. I+1). It loads those once and forms each fine
+// value with prolong_point3d's formula for its class (odd/even indices), in the same
+// order, so the result is bit-identical to k_prolong3d; points with exactly two even
+// indices are skipped unless bilinear (nu2 <= 0), as there. One thread per fine point
+// spent ~80 instructions per point on 64-bit index arithmetic and branches that diverge
+// between neighbouring points; here the arithmetic is shared by eight points.
+template <typename T>
+__global__ void __launch_bounds__(256) k_prolong3d_cells(Lvl<T> f, Lvl<T> c, int bilinear) {
+  pdl_enter();
+  const int I = 1 + blockIdx.x * blockDim.x + threadIdx.x;  // cells 1 .. m_c per axis
+  const int J = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  const int K = 1 + blockIdx.z;
+  if (I > c.mx || J > c.my) return;
+  const long long Sc = c.S;
+  const int Pc = c.P;
+  const T* pc = c.phi + (long long)K * Sc + (long long)J * Pc + I;
+  // corners: cabc = phi_c(K + a, J + b, I + c)
+  const T c000 = pc[0], c001 = pc[1], c010 = pc[Pc], c011 = pc[Pc + 1];
+  const T c100 = pc[Sc], c101 = pc[Sc + 1], c110 = pc[Sc + Pc], c111 = pc[Sc + Pc + 1];
+  const long long Sf = f.S;
+  const int Pf = f.P;
+  const int k0 = 2 * K - 1, j0 = 2 * J - 1, i0 = 2 * I - 1;  // the odd fine indices of the cell
+  T* pf = f.phi + (long long)k0 * Sf + (long long)j0 * Pf + i0;
+  const bool kin0 = k0 >= 2, jin0 = j0 >= 2, iin0 = i0 >= 2;  // the even ones (2K ...) are interior
+#define JMG_ADD(dk, dj, di, val)                                              \
+  {                                                                           \
+    T* q = pf + (dk) * Sf + (dj) * Pf + (di);                                 \
+    *q = *q + (val);                                                          \
+  }
+  // (odd, odd, odd): injection
+  if (kin0 && jin0 && iin0) JMG_ADD(0, 0, 0, c000);
+  // one even index: 0.5 (c(kp, jp, ip) + c(.. m ..)), the even axis taking K+1 and K
+  if (kin0 && jin0) JMG_ADD(0, 0, 1, T(0.5) * (c001 + c000));
+  if (kin0 && iin0) JMG_ADD(0, 1, 0, T(0.5) * (c010 + c000));
+  if (jin0 && iin0) JMG_ADD(1, 0, 0, T(0.5) * (c100 + c000));
+  // two even indices (bilinear), computed only when asked
+  if (bilinear) {
+    if (kin0) JMG_ADD(0, 1, 1, T(0.25) * (((c011 + c001) + c010) + c000));
+    if (jin0) JMG_ADD(1, 0, 1, T(0.25) * (((c101 + c001) + c100) + c000));
+    if (iin0) JMG_ADD(1, 1, 0, T(0.25) * (((c110 + c010) + c100) + c000));
+  }
+  // three even indices: the eight corners in prolong_point3d's order
+  {
+    T s = c111;
+    s = s + c011;
+    s = s + c101;
+    s = s + c001;
+    s = s + c110;
+    s = s + c010;
+    s = s + c100;
+    s = s + c000;
+    JMG_ADD(1, 1, 1, T(0.125) * s);
+  }
+#undef JMG_ADD
+}
+
 // Tiles: FP32 4 x 4 x 16 coarse points (256 threads, 27.6 KB of shared memory), FP64
 // 4 x 4 x 8 (128 threads, 29.4 KB).
 template <typename T>
@@ -162,6 +222,14 @@ void launch_restrict_tile3d(const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s) {
   launch_k(k_restrict_tile3d<T, CK, CJ, CI>, g, dim3(CK * CJ * CI), 0, s, f, c);
 }
 
+template <typename T>
+void launch_prolong_cells3d(const Lvl<T>& f, const Lvl<T>& c, int bilinear, cudaStream_t s) {
+  dim3 b(32, 8, 1), g((unsigned)((c.mx + 31) / 32), (unsigned)((c.my + 7) / 8), (unsigned)c.mz);
+  launch_k(k_prolong3d_cells<T>, g, b, 0, s, f, c, bilinear);
+}
+
+template void launch_prolong_cells3d<double>(const Lvl<double>&, const Lvl<double>&, int, cudaStream_t);
+template void launch_prolong_cells3d<float>(const Lvl<float>&, const Lvl<float>&, int, cudaStream_t);
 template void launch_restrict_tile3d<double>(const Lvl<double>&, const Lvl<double>&, cudaStream_t);
 template void launch_restrict_tile3d<float>(const Lvl<float>&, const Lvl<float>&, cudaStream_t);
 

@@ -39,7 +39,7 @@ def _problem(mx, my, mz, seed):
 
 
 def _solve(monkeypatch, env, grids, args, **opts):
-    for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_RESTRICT3D", "JMG_FUSED2D"):
+    for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_RESTRICT3D", "JMG_FUSED2D", "JMG_PROLONG3D"):
         monkeypatch.delenv(k, raising=False)
     for k, v in env.items():
         monkeypatch.setenv(k, v)
@@ -71,12 +71,14 @@ def test_one_pass_equals_colour_passes(monkeypatch, shape, opts):
     assert torch.equal(got, ref)
 
 
-@pytest.mark.parametrize("shape,opts", [CASES[0], CASES[2], CASES[6], CASES[7]])
+@pytest.mark.parametrize("shape,opts", [CASES[0], CASES[2], CASES[6], CASES[7],
+                                        ((64, 64, 32), dict(fixed=True, max_iters_outer=3, nu1=1, nu2=0))])
 def test_tiled_restriction_equals_grid_restriction(monkeypatch, shape, opts):
-    """The same solves with the tiled 3D restriction (default) and the grid-wide one."""
+    """The same solves with the tiled 3D restriction and the cell prolongation (defaults)
+    and with the grid-wide ones (nu2 = 0 makes the prolongation bilinear)."""
     grids = tuple(grid_1D(m) for m in shape)
     args = _problem(*shape, seed=7 + sum(shape))
-    ref, c_ref = _solve(monkeypatch, {"JMG_RESTRICT3D": "grid"}, grids, args, **opts)
+    ref, c_ref = _solve(monkeypatch, {"JMG_RESTRICT3D": "grid", "JMG_PROLONG3D": "grid"}, grids, args, **opts)
     got, c_got = _solve(monkeypatch, {}, grids, args, **opts)
     assert int(c_got) == int(c_ref)
     assert torch.equal(got, ref)
@@ -106,7 +108,7 @@ def test_one_pass_2d_equals_colour_passes(monkeypatch, shape, opts):
     grids = (grid_1D(mx), grid_1D(my))
 
     def run(env):
-        for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_RESTRICT3D", "JMG_FUSED2D"):
+        for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_RESTRICT3D", "JMG_FUSED2D", "JMG_PROLONG3D"):
             monkeypatch.delenv(k, raising=False)
         for k, v in env.items():
             monkeypatch.setenv(k, v)
