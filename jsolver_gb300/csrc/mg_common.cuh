@@ -280,6 +280,70 @@ __device__ __forceinline__ bool prolong_point3d(const Lvl<T>& c, int k, int j, i
   return true;
 }
 
+// Prolongation by coarse cells, the same values as prolong_point2d / prolong_point3d:
+// the fine points (2J-1 .. 2J, 2I-1 .. 2I[, 2K-1 .. 2K]) all interpolate from the coarse
+// corners (J .. J+1, I .. I+1[, K .. K+1]); the corners are loaded once and each fine
+// value takes its class's formula in the reference's order (solver_2d.py:649-668,
+// solver_3d.py:654-677). Neighbouring fine points belong to different classes, so one
+// thread per fine point diverges; one per cell does not. Cells run 1 .. m_c per axis.
+template <typename T>
+__device__ __forceinline__ void prolong_cell2d(const Lvl<T>& f, const Lvl<T>& c, int J, int I, bool diag) {
+  const int Pc = c.P;
+  const T* pc = c.phi + (long long)J * Pc + I;
+  const T c00 = pc[0], c01 = pc[1], c10 = pc[Pc], c11 = pc[Pc + 1];  // c_ab = phi_c(J + a, I + b)
+  const int Pf = f.P;
+  const int r0 = 2 * J - 1, q0 = 2 * I - 1;  // odd fine row and column of the cell
+  T* pf = f.phi + (long long)r0 * Pf + q0;
+  const bool rin = r0 >= 2, qin = q0 >= 2;   // the even ones (2J, 2I) are interior
+  if (rin && qin) pf[0] = pf[0] + c00;
+  if (rin) pf[1] = pf[1] + T(0.5) * (c01 + c00);    // odd row, even column
+  if (qin) pf[Pf] = pf[Pf] + T(0.5) * (c10 + c00);  // even row, odd column
+  if (diag) pf[Pf + 1] = pf[Pf + 1] + T(0.25) * (((c11 + c01) + c10) + c00);
+}
+
+template <typename T>
+__device__ __forceinline__ void prolong_cell3d(const Lvl<T>& f, const Lvl<T>& c, int K, int J, int I,
+                                               bool bilinear) {
+  const long long Sc = c.S;
+  const int Pc = c.P;
+  const T* pc = c.phi + (long long)K * Sc + (long long)J * Pc + I;
+  // corners: cabc = phi_c(K + a, J + b, I + c)
+  const T c000 = pc[0], c001 = pc[1], c010 = pc[Pc], c011 = pc[Pc + 1];
+  const T c100 = pc[Sc], c101 = pc[Sc + 1], c110 = pc[Sc + Pc], c111 = pc[Sc + Pc + 1];
+  const long long Sf = f.S;
+  const int Pf = f.P;
+  const int k0 = 2 * K - 1, j0 = 2 * J - 1, i0 = 2 * I - 1;  // the odd fine indices of the cell
+  T* pf = f.phi + (long long)k0 * Sf + (long long)j0 * Pf + i0;
+  const bool kin0 = k0 >= 2, jin0 = j0 >= 2, iin0 = i0 >= 2;  // the even ones are interior
+#define JMG_ADD(dk, dj, di, val)              \
+  {                                           \
+    T* q = pf + (dk) * Sf + (dj) * Pf + (di); \
+    *q = *q + (val);                          \
+  }
+  if (kin0 && jin0 && iin0) JMG_ADD(0, 0, 0, c000);  // (odd, odd, odd): injection
+  // one even index: 0.5 (c(kp, jp, ip) + c(.. m ..)), the even axis taking K+1 and K
+  if (kin0 && jin0) JMG_ADD(0, 0, 1, T(0.5) * (c001 + c000));
+  if (kin0 && iin0) JMG_ADD(0, 1, 0, T(0.5) * (c010 + c000));
+  if (jin0 && iin0) JMG_ADD(1, 0, 0, T(0.5) * (c100 + c000));
+  if (bilinear) {  // two even indices, computed only when asked
+    if (kin0) JMG_ADD(0, 1, 1, T(0.25) * (((c011 + c001) + c010) + c000));
+    if (jin0) JMG_ADD(1, 0, 1, T(0.25) * (((c101 + c001) + c100) + c000));
+    if (iin0) JMG_ADD(1, 1, 0, T(0.25) * (((c110 + c010) + c100) + c000));
+  }
+  {  // three even indices: the eight corners in prolong_point3d's order
+    T s = c111;
+    s = s + c011;
+    s = s + c101;
+    s = s + c001;
+    s = s + c110;
+    s = s + c010;
+    s = s + c100;
+    s = s + c000;
+    JMG_ADD(1, 1, 1, T(0.125) * s);
+  }
+#undef JMG_ADD
+}
+
 // Order-preserving bit pattern of |x| for NaN-propagating max reductions: for
 // non-negative doubles the IEEE bit pattern is monotone, and a NaN (sign cleared)
 // compares above +inf, so the maximum is NaN whenever any difference is NaN. This

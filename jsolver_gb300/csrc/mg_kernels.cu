@@ -184,18 +184,16 @@ __device__ void blk_restrict(const Lvl<T>& f, const Lvl<T>& c) {
   __syncthreads();
 }
 
+// by coarse cells (prolong_cell2d/3d): one thread updates the 4 (2D) or 8 (3D) fine
+// points of a cell from its corners, without divergence between classes
 template <typename T, int DIM>
 __device__ void blk_prolong(const Lvl<T>& f, const Lvl<T>& c, bool diag) {
-  const int nx = f.mx - 1, ny = f.my - 1, nz = DIM == 3 ? f.mz - 1 : 1;
+  const int nx = c.mx, ny = c.my, nz = DIM == 3 ? c.mz : 1;
   const int n = nx * ny * nz;
   for (int t = threadIdx.x; t < n; t += blockDim.x) {
-    const int i = 2 + t % nx, j = 2 + (t / nx) % ny, k = 2 + t / (nx * ny);
-    T v;
-    bool ok = DIM == 2 ? prolong_point2d<T>(c, j, i, diag, &v) : prolong_point3d<T>(c, k, j, i, diag, &v);
-    if (ok) {
-      const long long p = DIM == 2 ? (long long)j * f.P + i : (long long)k * f.S + (long long)j * f.P + i;
-      f.phi[p] = f.phi[p] + v;
-    }
+    const int I = 1 + t % nx, J = 1 + (t / nx) % ny, K = 1 + t / (nx * ny);
+    if (DIM == 2) prolong_cell2d<T>(f, c, J, I, diag);
+    else prolong_cell3d<T>(f, c, K, J, I, diag);
   }
   __syncthreads();
 }
@@ -431,6 +429,12 @@ void launch_restrict(int dim, const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s) 
 template <typename T>
 void launch_prolong(int dim, const Lvl<T>& f, const Lvl<T>& c, int diag, cudaStream_t s) {
   if (dim == 2) {
+    // by coarse cells (mg_tile2d.cu) unless JMG_PROLONG2D=grid; the same bits
+    const char* e2 = getenv("JMG_PROLONG2D");
+    if (!(e2 && std::strcmp(e2, "grid") == 0)) {
+      launch_prolong_cells2d<T>(f, c, diag, s);
+      return;
+    }
     dim3 b(64, 4), g(cdiv(f.mx - 1, 64), cdiv(f.my - 1, 4));
     launch_k(k_prolong2d<T>, g, b, 0, s, f, c, diag);
   } else {

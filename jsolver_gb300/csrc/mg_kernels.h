@@ -53,6 +53,7 @@ template <typename T> void launch_sweep_onepass2d(Lvl<T>& a, bool zero_in, cudaS
 template <typename T> void launch_sweep_onepass(int dim, Lvl<T>& a, bool zero_in, cudaStream_t s);
 template <typename T> void launch_restrict_tile3d(const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s);
 template <typename T> void launch_prolong_cells3d(const Lvl<T>& f, const Lvl<T>& c, int bilinear, cudaStream_t s);
+template <typename T> void launch_prolong_cells2d(const Lvl<T>& f, const Lvl<T>& c, int diag, cudaStream_t s);
 int fused_chunk3d(int mx, int my, int mz, int blocks_per_sm);
 int fused_blocks3d(int mx, int my, int mz);
 int fused_wave_permille(int mx, int my, int mz);

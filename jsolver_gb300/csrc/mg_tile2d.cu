@@ -185,6 +185,29 @@ void launch_restrict_tile2d(const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s) {
   launch_k(k_restrict_tile2d<T>, g, dim3(256), 0, s, f, c);
 }
 
+// phi_f += P phi_c (solver_2d.py:649-668) by coarse cells: a thread takes the fine rows
+// 2J-1 .. 2J and columns 2I-1 .. 2I, which interpolate from the four coarse corners
+// (J .. J+1, I .. I+1); it loads those once and forms each fine value with
+// prolong_point2d's formula for its class, in the same order (bit-identical to
+// k_prolong2d); the (even, even) points only with diag (nu2 <= 0 or D_xy).
+template <typename T>
+__global__ void __launch_bounds__(256) k_prolong2d_cells(Lvl<T> f, Lvl<T> c, int diag) {
+  pdl_enter();
+  const int I = 1 + blockIdx.x * blockDim.x + threadIdx.x;  // coarse column, 1 .. m_c
+  const int J = 1 + blockIdx.y * blockDim.y + threadIdx.y;  // coarse row
+  if (I > c.mx || J > c.my) return;
+  prolong_cell2d<T>(f, c, J, I, diag != 0);
+}
+
+template <typename T>
+void launch_prolong_cells2d(const Lvl<T>& f, const Lvl<T>& c, int diag, cudaStream_t s) {
+  dim3 b(32, 8), g((unsigned)((c.mx + 31) / 32), (unsigned)((c.my + 7) / 8));
+  launch_k(k_prolong2d_cells<T>, g, b, 0, s, f, c, diag);
+}
+
+template void launch_prolong_cells2d<double>(const Lvl<double>&, const Lvl<double>&, int, cudaStream_t);
+template void launch_prolong_cells2d<float>(const Lvl<float>&, const Lvl<float>&, int, cudaStream_t);
+
 template void launch_restrict_tile2d<double>(const Lvl<double>&, const Lvl<double>&, cudaStream_t);
 template void launch_restrict_tile2d<float>(const Lvl<float>&, const Lvl<float>&, cudaStream_t);
 

@@ -156,47 +156,7 @@ __global__ void __launch_bounds__(256) k_prolong3d_cells(Lvl<T> f, Lvl<T> c, int
   const int J = 1 + blockIdx.y * blockDim.y + threadIdx.y;
   const int K = 1 + blockIdx.z;
   if (I > c.mx || J > c.my) return;
-  const long long Sc = c.S;
-  const int Pc = c.P;
-  const T* pc = c.phi + (long long)K * Sc + (long long)J * Pc + I;
-  // corners: cabc = phi_c(K + a, J + b, I + c)
-  const T c000 = pc[0], c001 = pc[1], c010 = pc[Pc], c011 = pc[Pc + 1];
-  const T c100 = pc[Sc], c101 = pc[Sc + 1], c110 = pc[Sc + Pc], c111 = pc[Sc + Pc + 1];
-  const long long Sf = f.S;
-  const int Pf = f.P;
-  const int k0 = 2 * K - 1, j0 = 2 * J - 1, i0 = 2 * I - 1;  // the odd fine indices of the cell
-  T* pf = f.phi + (long long)k0 * Sf + (long long)j0 * Pf + i0;
-  const bool kin0 = k0 >= 2, jin0 = j0 >= 2, iin0 = i0 >= 2;  // the even ones (2K ...) are interior
-#define JMG_ADD(dk, dj, di, val)                                              \
-  {                                                                           \
-    T* q = pf + (dk) * Sf + (dj) * Pf + (di);                                 \
-    *q = *q + (val);                                                          \
-  }
-  // (odd, odd, odd): injection
-  if (kin0 && jin0 && iin0) JMG_ADD(0, 0, 0, c000);
-  // one even index: 0.5 (c(kp, jp, ip) + c(.. m ..)), the even axis taking K+1 and K
-  if (kin0 && jin0) JMG_ADD(0, 0, 1, T(0.5) * (c001 + c000));
-  if (kin0 && iin0) JMG_ADD(0, 1, 0, T(0.5) * (c010 + c000));
-  if (jin0 && iin0) JMG_ADD(1, 0, 0, T(0.5) * (c100 + c000));
-  // two even indices (bilinear), computed only when asked
-  if (bilinear) {
-    if (kin0) JMG_ADD(0, 1, 1, T(0.25) * (((c011 + c001) + c010) + c000));
-    if (jin0) JMG_ADD(1, 0, 1, T(0.25) * (((c101 + c001) + c100) + c000));
-    if (iin0) JMG_ADD(1, 1, 0, T(0.25) * (((c110 + c010) + c100) + c000));
-  }
-  // three even indices: the eight corners in prolong_point3d's order
-  {
-    T s = c111;
-    s = s + c011;
-    s = s + c101;
-    s = s + c001;
-    s = s + c110;
-    s = s + c010;
-    s = s + c100;
-    s = s + c000;
-    JMG_ADD(1, 1, 1, T(0.125) * s);
-  }
-#undef JMG_ADD
+  prolong_cell3d<T>(f, c, K, J, I, bilinear != 0);
 }
 
 // Tiles: FP32 4 x 4 x 16 coarse points (256 threads, 27.6 KB of shared memory), FP64

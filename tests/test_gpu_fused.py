@@ -39,7 +39,8 @@ def _problem(mx, my, mz, seed):
 
 
 def _solve(monkeypatch, env, grids, args, **opts):
-    for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_RESTRICT3D", "JMG_FUSED2D", "JMG_PROLONG3D"):
+    for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_RESTRICT3D", "JMG_FUSED2D", "JMG_PROLONG3D",
+                  "JMG_PROLONG2D"):
         monkeypatch.delenv(k, raising=False)
     for k, v in env.items():
         monkeypatch.setenv(k, v)
@@ -108,7 +109,8 @@ def test_one_pass_2d_equals_colour_passes(monkeypatch, shape, opts):
     grids = (grid_1D(mx), grid_1D(my))
 
     def run(env):
-        for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_RESTRICT3D", "JMG_FUSED2D", "JMG_PROLONG3D"):
+        for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_RESTRICT3D", "JMG_FUSED2D", "JMG_PROLONG3D",
+                  "JMG_PROLONG2D"):
             monkeypatch.delenv(k, raising=False)
         for k, v in env.items():
             monkeypatch.setenv(k, v)
@@ -119,5 +121,33 @@ def test_one_pass_2d_equals_colour_passes(monkeypatch, shape, opts):
     ref, c_ref = run({"JMG_FUSED": "0"})
     # every level of at least 1000 points sweeps in one pass, FP32 and FP64
     got, c_got = run({"JMG_FUSED_POINTS": "1000", "JMG_FUSED64": "1"})
+    assert int(c_got) == int(c_ref)
+    assert torch.equal(got, ref)
+
+
+@pytest.mark.parametrize("shape,opts", [CASES_2D[0], CASES_2D[2], CASES_2D[3],
+                                        ((128, 128), dict(fixed=True, max_iters_outer=3, nu1=1, nu2=0))])
+def test_cell_prolongation_2d_equals_grid(monkeypatch, shape, opts):
+    """2D solves with the cell prolongation (default) and the grid-wide one, bit for bit
+    (nu2 = 0 adds the (even, even) points)."""
+    from jsolver_gb300 import workloads as W
+    from jsolver_gb300.solver_2d import solve_2d
+    mx, my = shape
+    p = W.random_2d(max(mx, my), seed=2 * mx + my)
+    sl = (slice(0, my + 3), slice(0, mx + 3))
+    args = [torch.from_numpy(np.ascontiguousarray(p[k][sl])).to(DEV) for k in ("phi0", "rhs", "lam", "D_xx", "D_yy")]
+    grids = (grid_1D(mx), grid_1D(my))
+
+    def run(env):
+        for k in ("JMG_PROLONG2D",):
+            monkeypatch.delenv(k, raising=False)
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        _engine.CACHE.plans.clear()
+        _engine.CACHE.ws.clear()
+        return solve_2d(*grids, *args, **opts)
+
+    ref, c_ref = run({"JMG_PROLONG2D": "grid"})
+    got, c_got = run({})
     assert int(c_got) == int(c_ref)
     assert torch.equal(got, ref)
