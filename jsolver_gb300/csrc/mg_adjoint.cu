@@ -13,17 +13,16 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "../../include/jmg.h"
+#include "mg_adjoint_seg.h"
 #include "mg_kernels.h"
 #include "mg_plan.h"
 
 namespace jmg {
 
-struct AdjLvl {
-  double *pb, *rb, *T, *gacc, *gwx, *gwy;
-};
 void adj_sweep(const Lvl<double>& a, const AdjLvl& g, const double* before, const double* after, cudaStream_t s);
 void adj_restrict(const Lvl<double>& a, const AdjLvl& g, const double* phi, const Lvl<double>& c, const AdjLvl& gc,
                   cudaStream_t s);
@@ -35,7 +34,7 @@ int set_error_message(int code, const char* msg);
 
 namespace {
 
-enum { OP_SWEEP = 0, OP_RESTRICT = 1, OP_PROLONG = 2 };
+enum { OP_SWEEP = kAdjOpSweep, OP_RESTRICT = kAdjOpRestrict, OP_PROLONG = kAdjOpProlong };
 constexpr int kZeros = -1;  // phi of a coarse level right after the restriction zeroed it
 constexpr int kInput = -2;  // phi of level 0 at the start of the cycle (the checkpoint)
 
@@ -46,7 +45,34 @@ struct TapeOp {
 struct Tape {
   std::vector<TapeOp> ops;
   std::vector<int> snap_lev;  // level of every snapshot
+  // maximal runs [first, last] of operators on the small levels (at most 2048 padded
+  // points, never level 0), each run by one block in one launch
+  std::vector<std::pair<int, int>> segs;
 };
+
+// first level a single block takes: the rule of the solve's coarse kernel, from level 1
+int adj_block_start(const JmgPlan* p) {
+  for (int l = 1; l < p->used; ++l) {
+    const long long pts = (long long)p->lv[l].box.nx * p->lv[l].box.ny * p->lv[l].box.nz;
+    if (pts <= 2048) return l;
+  }
+  return p->used;  // none
+}
+
+void find_segments(const JmgPlan* p, Tape& t) {
+  const int cs = adj_block_start(p);
+  const int n = (int)t.ops.size();
+  for (int k = 0; k < n;) {
+    if (t.ops[k].lev < cs) {
+      ++k;
+      continue;
+    }
+    int e = k;
+    while (e + 1 < n && t.ops[e + 1].lev >= cs) ++e;
+    if (e - k + 1 <= kMaxSegOps) t.segs.push_back({k, e});  // longer runs stay grid-wide
+    k = e + 1;
+  }
+}
 
 // the forward schedule of one cycle (solver_2d.py:582-614), with the phi state each
 // operator reads (before) and writes (after) as snapshot indices
@@ -81,6 +107,7 @@ Tape make_tape(const JmgPlan* p) {
   std::vector<int> cur(p->used, kZeros);
   cur[0] = kInput;
   tape_cycle(p, t, cur, 0, p->cfg.fcycle != 0, p->cfg.skip_pre != 0);
+  find_segments(p, t);
   return t;
 }
 
@@ -91,6 +118,8 @@ struct AdjLayout {
   size_t ckpt = 0;           // (n + 1) level-0 arrays
   size_t zeros = 0;          // one level-0 array of zeros
   size_t pre = 0;            // skip_pre: phi after each initial sweep (nu1 level-0 arrays)
+  size_t tabs = 0;           // AdjTables of the single-block segments
+  size_t segs = 0;           // one AdjSeg per segment
   int ncyc = 0;
 };
 
@@ -109,6 +138,8 @@ AdjLayout adj_layout(const JmgPlan* p, const Tape& t) {
   L.zeros = take(p->lv[0].elems * 8);
   const int nu1 = p->cfg.nu1 > 0 ? p->cfg.nu1 : 0;
   L.pre = take((size_t)(p->cfg.skip_pre ? nu1 + 1 : 1) * p->lv[0].elems * 8);
+  L.tabs = take(sizeof(AdjTables));
+  L.segs = take(sizeof(AdjSeg) * (t.segs.empty() ? 1 : t.segs.size()));
   L.total = off;
   return L;
 }
@@ -135,7 +166,15 @@ void run_tape_forward(const JmgPlan* p, void* ws, void* aws, const AdjLayout& L,
   // current buffer of every level (one-pass sweeps swap a level's two buffers)
   std::vector<Lvl<double>> cur(p->used);
   for (int l = 0; l < p->used; ++l) cur[l] = lvl64(p, ws, l);
-  for (const TapeOp& op : t.ops) {
+  size_t next_seg = 0;
+  for (int k = 0; k < (int)t.ops.size(); ++k) {
+    if (next_seg < t.segs.size() && t.segs[next_seg].first == k) {  // a single-block run
+      adj_seg_fwd(ptr<AdjTables>(aws, L.tabs), ptr<AdjSeg>(aws, L.segs) + next_seg, snapshots, cp.diag, s);
+      k = t.segs[next_seg].second;
+      ++next_seg;
+      continue;
+    }
+    const TapeOp& op = t.ops[k];
     Lvl<double>& a = cur[op.lev];
     if (op.kind == OP_SWEEP) launch_sweep<double>(p->dim, a, s);
     else if (op.kind == OP_RESTRICT) launch_restrict<double>(p->dim, a, cur[op.lev + 1], s);
@@ -159,6 +198,32 @@ void adj_core(const JmgPlan* p, void* ws, void* aws, const AdjLayout& L, const T
   const CycleParams cp = cycle_params(p, false);
   const int nu1 = p->cfg.nu1 > 0 ? p->cfg.nu1 : 0;
   double* pre = ptr<double>(aws, L.pre);
+  const double* zeros = ptr<double>(aws, L.zeros);
+  // the single-block segments' tables and operators, their phi states resolved (segments
+  // hold no level-0 operator, so no state depends on the cycle's checkpoint)
+  if (!tape.segs.empty()) {
+    AdjTables tabs;
+    memset(&tabs, 0, sizeof(tabs));
+    for (int l = 0; l < p->used; ++l) {
+      tabs.lv.l[l] = lvl64(p, ws, l);
+      tabs.g[l] = adj_lvl(p, aws, L, l);
+    }
+    adj_store_tables(tabs, ptr<AdjTables>(aws, L.tabs), s);
+    for (size_t q = 0; q < tape.segs.size(); ++q) {
+      AdjSeg sg;
+      memset(&sg, 0, sizeof(sg));
+      sg.n = tape.segs[q].second - tape.segs[q].first + 1;
+      for (int k = 0; k < sg.n; ++k) {
+        const TapeOp& op = tape.ops[tape.segs[q].first + k];
+        AdjSegOp& o = sg.op[k];
+        o.kind = op.kind;
+        o.lev = op.lev;
+        o.before = op.before == kZeros ? zeros : op.before >= 0 ? ptr<double>(aws, L.snap[op.before]) : nullptr;
+        o.after = op.kind != OP_RESTRICT ? ptr<double>(aws, L.snap[op.after]) : nullptr;
+      }
+      adj_store_seg(sg, ptr<AdjSeg>(aws, L.segs) + q, s);
+    }
+  }
   if (p->cfg.skip_pre) {  // the one-off pre-smoothing (solver_2d.py:457-459)
     cudaMemcpyAsync(pre, l0.phi, e0 * 8, cudaMemcpyDeviceToDevice, s);
     Lvl<double> cur = l0;
@@ -176,7 +241,6 @@ void adj_core(const JmgPlan* p, void* ws, void* aws, const AdjLayout& L, const T
   }
   std::vector<AdjLvl> g(p->used);
   for (int l = 0; l < p->used; ++l) g[l] = adj_lvl(p, aws, L, l);
-  const double* zeros = ptr<double>(aws, L.zeros);
   for (int k = L.ncyc - 1; k >= 0; --k) {
     cudaMemcpyAsync(l0.phi, ck + (size_t)k * e0, e0 * 8, cudaMemcpyDeviceToDevice, s);
     run_tape_forward(p, ws, aws, L, tape, true, s);
@@ -185,7 +249,14 @@ void adj_core(const JmgPlan* p, void* ws, void* aws, const AdjLayout& L, const T
       if (idx == kInput) return ck + (size_t)k * e0;
       return ptr<double>(aws, L.snap[idx]);
     };
+    int seg = (int)tape.segs.size() - 1;
     for (int t = (int)tape.ops.size() - 1; t >= 0; --t) {
+      if (seg >= 0 && tape.segs[seg].second == t) {  // a single-block run, in reverse
+        adj_seg_rev(ptr<AdjTables>(aws, L.tabs), ptr<AdjSeg>(aws, L.segs) + seg, cp.diag, s);
+        t = tape.segs[seg].first;
+        --seg;
+        continue;
+      }
       const TapeOp& op = tape.ops[t];
       Lvl<double> a = lvl64(p, ws, op.lev);
       if (op.kind == OP_SWEEP) {

@@ -9,14 +9,13 @@
 // transpose: t = pb[p] / A_cc(p); rb[p] -= t; gacc[p] -= t phi_new[p]; gw_pq += t phi_q;
 // pb[q] += w_pq t for the neighbours q (other colour); pb[p] = 0. Each face joins one red
 // and one black point, so within a colour every face gradient has a single writer.
+#include "mg_adjoint_seg.h"
+#include "mg_block.cuh"
 #include "mg_common.cuh"
 #include "mg_kernels.h"
 
 namespace jmg {
 
-struct AdjLvl {
-  double *pb, *rb, *T, *gacc, *gwx, *gwy;
-};
 
 static inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
@@ -27,12 +26,12 @@ __device__ __forceinline__ bool colour_point(const Lvl<double>& a, int c, int& i
   return i <= a.my && j <= a.mx;
 }
 
-// transpose of one colour update, part 1: scale, rhs / coefficient adjoints, clear pb
-// nb: phi values the forward update read at the neighbours; nw: phi after the update
-__global__ void k_adj_colour_scale(Lvl<double> a, AdjLvl g, int c, const double* __restrict__ nb,
-                                   const double* __restrict__ nw) {
-  int i, j;
-  if (!colour_point(a, c, i, j)) return;
+// ---- per-point bodies (the grid kernels and the single-block segments share them) ----
+
+// transpose of one colour update, part 1, at (i, j): scale, rhs / coefficient adjoints,
+// clear pb. nb: phi values the forward update read at the neighbours; nw: phi after it
+__device__ __forceinline__ void adj_scale_pt(const Lvl<double>& a, const AdjLvl& g, int i, int j,
+                                             const double* __restrict__ nb, const double* __restrict__ nw) {
   const int P = a.P;
   const long long p = (long long)i * P + j;
   const double t = g.pb[p] * a.invd[p];
@@ -48,21 +47,18 @@ __global__ void k_adj_colour_scale(Lvl<double> a, AdjLvl g, int c, const double*
 
 // transpose of one colour update, part 2: the other colour gathers w_pq t_p (sign +1) or,
 // for the defect, -w_pq d_p (sign -1)
-__global__ void k_adj_gather(Lvl<double> a, AdjLvl g, int c, double sign) {
-  int i, j;
-  if (!colour_point(a, c, i, j)) return;
+__device__ __forceinline__ void adj_gather_pt(const Lvl<double>& a, const AdjLvl& g, int i, int j, double sign) {
   const int P = a.P;
   const long long q = (long long)i * P + j;
   const double s = a.wx[q - 1] * g.T[q - 1] + a.wx[q] * g.T[q + 1] + a.wy[q - P] * g.T[q - P] + a.wy[q] * g.T[q + P];
   g.pb[q] += sign * s;
 }
 
-// transpose of defect + restriction, part 1, at the red points p (the only ones the
+// transpose of defect + restriction, part 1, at the red point (i, j) (the only ones the
 // restriction reads): d_bar = R^T rc_bar; rb += d_bar; pb += A_cc d_bar; coefficient adjoints
-__global__ void k_adj_restrict_red(Lvl<double> a, AdjLvl g, const double* __restrict__ phi, Lvl<double> c,
-                                   const double* __restrict__ rbc) {
-  int i, j;
-  if (!colour_point(a, 0, i, j)) return;
+__device__ __forceinline__ void adj_restrict_red_pt(const Lvl<double>& a, const AdjLvl& g,
+                                                    const double* __restrict__ phi, const Lvl<double>& c,
+                                                    const double* __restrict__ rbc, int i, int j) {
   const int P = a.P, Pc = c.P;
   const long long p = (long long)i * P + j;
   double db = 0.0;
@@ -88,12 +84,10 @@ __global__ void k_adj_restrict_red(Lvl<double> a, AdjLvl g, const double* __rest
   g.gwy[p] -= db * phi[p + P];
 }
 
-// transpose of phi_f += P(phi_c): pb_c = P^T pb_f over the coarse interior; also clears
-// rb_c (a new coarse visit starts) and zeroes both on the coarse frame
-__global__ void k_adj_prolong(Lvl<double> f, AdjLvl gf, Lvl<double> c, AdjLvl gc, int diag) {
-  const int I = blockIdx.x * blockDim.x + threadIdx.x;
-  const int J = blockIdx.y * blockDim.y + threadIdx.y;
-  if (I > c.mx + 2 || J > c.my + 2) return;
+// transpose of phi_f += P(phi_c) at the coarse point (J, I) of the padded box: pb_c =
+// P^T pb_f inside; also clears rb_c (a new coarse visit starts); zero on the frame
+__device__ __forceinline__ void adj_prolong_pt(const Lvl<double>& f, const AdjLvl& gf, const Lvl<double>& c,
+                                               const AdjLvl& gc, int diag, int J, int I) {
   const long long q = (long long)J * c.P + I;
   double s = 0.0;
   if (J >= 2 && J <= c.my && I >= 2 && I <= c.mx) {
@@ -107,6 +101,32 @@ __global__ void k_adj_prolong(Lvl<double> f, AdjLvl gf, Lvl<double> c, AdjLvl gc
   }
   gc.pb[q] = s;
   gc.rb[q] = 0.0;
+}
+
+// ---- grid-wide kernels ----------------------------------------------------------------
+
+__global__ void k_adj_colour_scale(Lvl<double> a, AdjLvl g, int c, const double* __restrict__ nb,
+                                   const double* __restrict__ nw) {
+  int i, j;
+  if (colour_point(a, c, i, j)) adj_scale_pt(a, g, i, j, nb, nw);
+}
+
+__global__ void k_adj_gather(Lvl<double> a, AdjLvl g, int c, double sign) {
+  int i, j;
+  if (colour_point(a, c, i, j)) adj_gather_pt(a, g, i, j, sign);
+}
+
+__global__ void k_adj_restrict_red(Lvl<double> a, AdjLvl g, const double* __restrict__ phi, Lvl<double> c,
+                                   const double* __restrict__ rbc) {
+  int i, j;
+  if (colour_point(a, 0, i, j)) adj_restrict_red_pt(a, g, phi, c, rbc, i, j);
+}
+
+__global__ void k_adj_prolong(Lvl<double> f, AdjLvl gf, Lvl<double> c, AdjLvl gc, int diag) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  if (I > c.mx + 2 || J > c.my + 2) return;
+  adj_prolong_pt(f, gf, c, gc, diag, J, I);
 }
 
 // backward of the coefficient hierarchy of level l (solver_2d.py:326-421): A_cc adjoints
@@ -172,6 +192,112 @@ void adj_hierarchy2d(const Lvl<double>& a, const AdjLvl& g, int level, double sx
                      double* dby, double* dlam, cudaStream_t s) {
   dim3 b(32, 8), gr(cdiv(a.mx + 3, 32), cdiv(a.my + 3, 8));
   k_adj_hierarchy2d<<<gr, b, 0, s>>>(a, g, level, sx, sy, nx0, dbx, dby, dlam);
+}
+
+// ---- single-block segments ------------------------------------------------------------
+// A run of tape operators on the small levels (one block's worth of points) executes in
+// one launch: the forward with its snapshots, or the reverse, one pass per barrier. The
+// passes evaluate the per-point bodies above (adjoint) and mg_block.cuh (forward), the
+// same as the grid-wide kernels, so the results are the same bits.
+
+template <typename F>
+__device__ __forceinline__ void blk_colour(const Lvl<double>& a, int c, F&& body) {
+  const int hx = a.mx / 2, n = hx * (a.my - 1);
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    const int i = 2 + t / hx;
+    const int j = 2 + ((i + c) & 1) + 2 * (t % hx);
+    if (j <= a.mx) body(i, j);
+  }
+  __syncthreads();
+}
+
+__device__ void blk_adj_sweep(const Lvl<double>& a, const AdjLvl& g, const double* before, const double* after) {
+  // reverse of the forward order: black (colour 1) then red (colour 0)
+  blk_colour(a, 1, [&](int i, int j) { adj_scale_pt(a, g, i, j, after, after); });
+  blk_colour(a, 0, [&](int i, int j) { adj_gather_pt(a, g, i, j, 1.0); });
+  blk_colour(a, 0, [&](int i, int j) { adj_scale_pt(a, g, i, j, before, after); });
+  blk_colour(a, 1, [&](int i, int j) { adj_gather_pt(a, g, i, j, 1.0); });
+}
+
+__device__ void blk_adj_restrict(const Lvl<double>& a, const AdjLvl& g, const double* phi, const Lvl<double>& c,
+                                 const AdjLvl& gc) {
+  blk_colour(a, 0, [&](int i, int j) { adj_restrict_red_pt(a, g, phi, c, gc.rb, i, j); });
+  blk_colour(a, 1, [&](int i, int j) { adj_gather_pt(a, g, i, j, -1.0); });
+}
+
+__device__ void blk_adj_prolong(const Lvl<double>& f, const AdjLvl& gf, const Lvl<double>& c, const AdjLvl& gc,
+                                int diag) {
+  const int nx = c.mx + 3, n = nx * (c.my + 3);
+  for (int t = threadIdx.x; t < n; t += blockDim.x) adj_prolong_pt(f, gf, c, gc, diag, t / nx, t % nx);
+  __syncthreads();
+}
+
+// the tables and the segment, staged in shared memory (they are read at every operator)
+struct AdjSegStage {
+  AdjTables tab;
+  AdjSeg seg;
+};
+
+__device__ void stage_seg(AdjSegStage* st, const AdjTables* tabs, const AdjSeg* seg) {
+  const int n1 = (int)(sizeof(AdjTables) / sizeof(int)), n2 = (int)(sizeof(AdjSeg) / sizeof(int));
+  const int* a = reinterpret_cast<const int*>(tabs);
+  const int* b = reinterpret_cast<const int*>(seg);
+  int* da = reinterpret_cast<int*>(&st->tab);
+  int* db = reinterpret_cast<int*>(&st->seg);
+  for (int k = threadIdx.x; k < n1; k += blockDim.x) da[k] = a[k];
+  for (int k = threadIdx.x; k < n2; k += blockDim.x) db[k] = b[k];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(1024) k_adj_seg_fwd(const AdjTables* tabs, const AdjSeg* seg, int snapshots,
+                                                     int diag) {
+  __shared__ AdjSegStage st;
+  stage_seg(&st, tabs, seg);
+  for (int o = 0; o < st.seg.n; ++o) {
+    const AdjSegOp op = st.seg.op[o];
+    const Lvl<double>& a = st.tab.lv.l[op.lev];
+    if (op.kind == kAdjOpRestrict) {
+      blk_restrict<double, 2>(a, st.tab.lv.l[op.lev + 1]);
+      continue;
+    }
+    if (op.kind == kAdjOpSweep) blk_sweep<double, 2>(a);
+    else blk_prolong<double, 2>(a, st.tab.lv.l[op.lev + 1], diag != 0);
+    if (snapshots) {
+      const int n = a.P * (a.my + 3);
+      for (int t = threadIdx.x; t < n; t += blockDim.x) op.after[t] = a.phi[t];
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_adj_seg_rev(const AdjTables* tabs, const AdjSeg* seg, int diag) {
+  __shared__ AdjSegStage st;
+  stage_seg(&st, tabs, seg);
+  for (int o = st.seg.n - 1; o >= 0; --o) {
+    const AdjSegOp op = st.seg.op[o];
+    const Lvl<double>& a = st.tab.lv.l[op.lev];
+    const AdjLvl& g = st.tab.g[op.lev];
+    if (op.kind == kAdjOpSweep) blk_adj_sweep(a, g, op.before, op.after);
+    else if (op.kind == kAdjOpProlong) blk_adj_prolong(a, g, st.tab.lv.l[op.lev + 1], st.tab.g[op.lev + 1], diag);
+    else blk_adj_restrict(a, g, op.before, st.tab.lv.l[op.lev + 1], st.tab.g[op.lev + 1]);
+  }
+}
+
+template <typename V>
+__global__ void k_adj_store(V v, V* dst) {
+  const int n = (int)(sizeof(V) / sizeof(int));
+  const int* src = reinterpret_cast<const int*>(&v);
+  int* d = reinterpret_cast<int*>(dst);
+  for (int k = threadIdx.x; k < n; k += blockDim.x) d[k] = src[k];
+}
+
+void adj_store_tables(const AdjTables& t, AdjTables* dst, cudaStream_t s) { k_adj_store<<<1, 256, 0, s>>>(t, dst); }
+void adj_store_seg(const AdjSeg& g, AdjSeg* dst, cudaStream_t s) { k_adj_store<<<1, 256, 0, s>>>(g, dst); }
+void adj_seg_fwd(const AdjTables* t, const AdjSeg* g, bool snapshots, int diag, cudaStream_t s) {
+  k_adj_seg_fwd<<<1, 1024, 0, s>>>(t, g, snapshots ? 1 : 0, diag);
+}
+void adj_seg_rev(const AdjTables* t, const AdjSeg* g, int diag, cudaStream_t s) {
+  k_adj_seg_rev<<<1, 1024, 0, s>>>(t, g, diag);
 }
 
 }  // namespace jmg
