@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -50,11 +51,17 @@ struct Tape {
   std::vector<std::pair<int, int>> segs;
 };
 
-// first level a single block takes: the rule of the solve's coarse kernel, from level 1
+// first level a single block takes: at most JMG_ADJ_BLOCK_POINTS padded points (2048 by
+// default, the rule of the solve's coarse kernel), from level 1
 int adj_block_start(const JmgPlan* p) {
+  static const long long limit = [] {
+    const char* e = getenv("JMG_ADJ_BLOCK_POINTS");
+    const long long v = e ? atoll(e) : 0;
+    return v > 0 ? v : 2048LL;
+  }();
   for (int l = 1; l < p->used; ++l) {
     const long long pts = (long long)p->lv[l].box.nx * p->lv[l].box.ny * p->lv[l].box.nz;
-    if (pts <= 2048) return l;
+    if (pts <= limit) return l;
   }
   return p->used;  // none
 }
