@@ -42,9 +42,13 @@ def _grids(m, xb, xe, centered):
 def _run(grids, phi0, rhs, lam, D, D_xy, opts):
     kw = dict(zip(_OPTION_NAMES, opts))
     phi, count = _engine.solve(grids, phi0, rhs, lam, D, D_xy, **kw)
+    # host tensors are solved on the GPU and come back as NumPy: return them as tensors
+    # on phi0's device, like the inputs
+    if not isinstance(phi, torch.Tensor):
+        phi = torch.from_numpy(phi).to(phi0.device)
     if not isinstance(count, torch.Tensor):
-        count = torch.tensor(count, dtype=torch.int64, device=phi.device)
-    return phi, count.reshape(())
+        count = torch.tensor(count, dtype=torch.int64, device=phi0.device)
+    return phi, count.to(phi0.device).reshape(())
 
 
 @torch.library.custom_op("jmg::solve_2d", mutates_args=())

@@ -59,6 +59,12 @@ def test_operators_match_solve_and_opcheck():
                                     *torch_ops.options())
     ref, rc = solve_2d(g, g, args[0], args[1], 0.5, args[3], args[4])
     assert torch.equal(phi, ref) and int(c) == int(rc)
+    # host tensors: solved on the GPU, returned on the host
+    cpu = [a.cpu() for a in args]
+    phi, c = torch.ops.jmg.solve_2d(*cpu, None, *torch_ops.grid_args(g, g), *torch_ops.options())
+    ref, rc = solve_2d(g, g, *args)
+    assert phi.device.type == "cpu" and c.device.type == "cpu"
+    assert torch.equal(phi, ref.cpu()) and int(c) == int(rc)
     torch.library.opcheck(torch.ops.jmg.solve_2d.default,
                           (*args, None, *torch_ops.grid_args(g, g), *torch_ops.options()),
                           test_utils=("test_schema", "test_faketensor"))
