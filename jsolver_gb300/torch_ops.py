@@ -4,9 +4,10 @@
 ``solver_3d.solve_3d`` (jsolver/solver_2d.py:196-236, solver_3d.py:196-237), so that
 torch code can put the solve into graphs that ``torch.compile`` or ``torch.export``
 trace: each has a fake (shape-only) implementation for tracing and runs the CUDA solve on
-the inputs' device and current stream. Grids are passed as per-axis (m, xb, xe, centered)
-lists; coefficients as tensors, 0-d for a scalar. The operators return ``(phi, count)``
-with ``count`` a 0-d int64 tensor on the same device. Reverse-mode differentiation is
+the inputs' device and current stream (host tensors are solved on the current GPU and
+returned on the host). Grids are passed as per-axis (m, xb, xe, centered) lists;
+coefficients as tensors, 0-d for a scalar. The operators return ``(phi, count)`` with
+``count`` a 0-d int64 tensor on the inputs' device. Reverse-mode differentiation is
 not registered here: it goes through ``solve_2d(..., fixed=True)`` (jsolver_gb300.adjoint).
 
 Example::
