@@ -11,7 +11,8 @@ network's initial guess, whose computation is inside every timed step. ``--outer
 ``richardson`` iterates the cycle as the reference does; ``fcg`` uses the same cycle as
 the preconditioner of flexible CG. The default is the headline form, mixed precision
 with FCG; every run also times the reference's plain FP64 iteration of the same problem
-the same way and reports it under ``plain_fp64``.
+the same way and reports it under ``plain_fp64``, and in 2D the same form from the
+learned guess under ``learned_guess_form`` (the learned + FP32 vs plain FP64 pairing).
 
 Our arm (default): ``value`` is the device time of a solve with inputs resident in HBM,
 through the C ABI (jmg_solve), timed with CUDA events on the solving stream; L2 is
@@ -478,6 +479,18 @@ def main():
             guess_rel_res = rel_residual(plan, wsb)
             solve_dev(stream)
         err_exact = (float(np.abs(out.cpu().numpy() - p["phi_exact"]).max()) if "phi_exact" in p else None)
+        # the metric's other pairing, learned guess + the same form, timed the same way (2D:
+        # the network is 2D); its guess is computed inside every timed solve
+        learned_cmp = None
+        if not args.no_compare and dim == 2 and not learned:
+            from jsolver_gb300.learned import GuessNet, WEIGHTS
+            if os.path.exists(WEIGHTS):
+                net = GuessNet.load(WEIGHTS, device=dev)
+                ms_l = timed(lambda s_: solve_dev(s_, plan, wsb, True), args.steps)
+                learned_cmp = {"form": f"learned guess + {args.form}", "ms": ms_l,
+                               "cycles": int(count.item()) * (args.inner_cycles if precision == "mixed" else 1),
+                               "final_rel_residual": rel_residual(plan, wsb),
+                               "speedup_vs_plain_fp64": (plain["ms"] / ms_l) if plain else None}
 
         # the fine-level red-black sweep of the form's cycles (FP64, or FP32 in the mixed
         # forms; one launch per sweep where the level sweeps in one pass, else two colour
@@ -574,6 +587,7 @@ def main():
         "plain_fp64": plain,
         "speedup_vs_plain_fp64": (plain["ms"] / ms) if plain else None,
         "guess_rel_residual": guess_rel_res,
+        "learned_guess_form": learned_cmp,
         "max_err_vs_exact_discrete": err_exact,
         "roofline": {"bound": "hbm",
                      "kernel": (f"{'k_sweep_fused3d' if dim == 3 else 'k_sweep_onepass2d'}"
