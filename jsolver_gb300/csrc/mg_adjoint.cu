@@ -10,6 +10,11 @@
 //             transposed; finally the backward of the coefficient hierarchy.
 // Outputs: adjoints of phi0, rhs, lambda, D_xx, D_yy (dense arrays, like the inputs). The
 // frame of phi is reset by do_BCs at every sweep and cycle, so its adjoint there is zero.
+// The checkpointed forward and the reverse sweep are captured once into a CUDA graph per
+// (workspace, adjoint workspace) pair. Within a cycle, each run of operators on the small
+// levels (at most 2048 points, below level 0) is one single-block launch forward (with its
+// snapshots) and one in reverse (mg_adjoint_kernels.cu), instead of a few launches per
+// operator.
 #include <cuda_runtime.h>
 
 #include <cmath>
