@@ -1,9 +1,12 @@
-"""Benchmark: ms to relative residual 1e-10 on the 2D 1024^2 random-coefficient problem.
+"""Benchmark: ms to relative residual 1e-10 on the 2D 1024^2 and 3D 256^3 random-coefficient problems.
 
 One step = one complete solve (coefficient hierarchy + cycles until
 ||rhs - L_h phi||_2 / ||rhs||_2 <= 1e-10) of the seeded synthetic problem
 ``jsolver_gb300.workloads.random_2d(1024, seed)``: D_xx, D_yy = exp(GRF sigma 1, corr.
-length 0.05), lambda ~ U[0, 10], rhs = L_h sin(pi x) sin(2 pi y).
+length 0.05), lambda ~ U[0, 10], rhs = L_h sin(pi x) sin(2 pi y). The default run also
+measures the 3D half of the metric, ``workload_3d``: ``random_3d(256, seed)`` (D = exp(GRF
+sigma 1.2, l 0.08) per axis, lambda = exp(GRF) scaled to [0, 50], rhs = smooth GRF noise
++ a Gaussian source), F-cycles, with the same keys as the 2D line.
 
 Forms (``--form``): ``fp64`` plain FP64 multigrid from phi0 = 0; ``mixed`` FP32 cycles in
 FP64 iterative refinement; ``learned`` / ``learned-mixed`` the same from the learned
@@ -17,13 +20,17 @@ learned guess under ``learned_guess_form`` (the learned + FP32 vs plain FP64 pai
 Our arm (default): ``value`` is the device time of a solve with inputs resident in HBM,
 through the C ABI (jmg_solve), timed with CUDA events on the solving stream; L2 is
 flushed (256 MB write) before every timed solve. ``e2e`` is the same solve through the
-public API (solve_2d on CUDA tensors) with the host->device copies of the inputs from
-pinned memory and the device->host copy of phi and the count inside the timed region.
-``--gpus N`` under torchrun runs N independent replicas (the path does not shard).
+public API (solve_2d / solve_3d on CUDA tensors) with the host->device copies of the
+inputs from pinned memory and the device->host copy of phi and the count inside the
+timed region. ``roofline`` is the kernel with the largest share of the solve in the
+committed launch list (profiles/launch_shares.json), timed alone with CUDA events;
+``roofline_fine_sweep`` the fine-level sweep beside it. ``cpu_baseline`` is the median
+time of full solves of the C oracle on all host cores. ``--gpus N`` under torchrun runs
+N independent replicas (the path does not shard).
 
 Reference arm (``--impl reference``): the reference's CPU path cannot run here (JAX is
 absent), so the oracle's C/OpenMP restatement of it is timed on the host cores, full
-solves, same workload and metric.
+solves, same workload and metric (and one full 3D solve under ``workload_3d``).
 """
 import argparse
 import ctypes
@@ -70,6 +77,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-3d", action="store_true", help="default run: skip the 3D 256^3 block (workload_3d)")
     ap.add_argument("--batch", type=int, default=64, help="problems per step of the batch workload")
     ap.add_argument("--iters", type=int, default=12, help="fixed cycles of the adjoint workload")
     ap.add_argument("--lanes", type=int, default=8, help="concurrent lanes of the batch workload")
@@ -165,22 +173,53 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def cpu_full_solves(p, dim, m, kw, runs, budget_s):
+    """Median time of full solves (phi0 = 0 to rel. residual 1e-10, plain FP64 cycles: the
+    reference's algorithm) of the C oracle on all host cores: `runs` solves, or fewer once
+    `budget_s` seconds have been spent (at least one)."""
+    from oracle import c_oracle
+    from oracle.grid import OracleGrid1D
+    g = OracleGrid1D(m)
+    nthreads = os.cpu_count() or 1
+    times, counts, rr = [], [], None
+    t_start = time.perf_counter()
+    for _ in range(max(1, runs)):
+        t0 = time.perf_counter()
+        _, cnt, rr = c_oracle.solve((g,) * dim, p["phi0"], p["rhs"], p["lam"], tuple(p[k] for k in coeff_names(dim)),
+                                    stop="residual", rtol=RTOL, nthreads=nthreads, **kw)
+        times.append((time.perf_counter() - t0) * 1e3)
+        counts.append(cnt)
+        if time.perf_counter() - t_start > budget_s:
+            break
+    return float(np.median(times)), len(times), counts[-1], rr, nthreads
+
+
+def cpu_baseline(p, dim, m, kw, runs, budget_s):
+    """The reported CPU baseline: the full-solve median of cpu_full_solves."""
+    ms, n, cycles, rr, nthreads = cpu_full_solves(p, dim, m, kw, runs, budget_s)
+    return {"value": ms, "unit": "ms", "cores": nthreads, "kind": "port",
+            "sample": f"median of {n} full solve(s) to rel. residual 1e-10 ({cycles} plain FP64 "
+                      f"{'V' if not kw else 'F' if kw.get('fcycle') else 'W'}-cycles from phi0 = 0), C/OpenMP "
+                      f"restatement of the reference algorithm (oracle/jmg_oracle.c), {nthreads} threads"}
+
+
 def reference_arm(args):
+    """The reference's algorithm on the host cores: full solves of the C oracle."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
+    p = make_problem(args, args.seed)
+    nthreads = os.cpu_count() or 1
+    kw = cycle_kw(args.cycle)
     from oracle import c_oracle
     from oracle.grid import OracleGrid1D
-    p = make_problem(args, args.seed)
     g = OracleGrid1D(args.m)
-    nthreads = os.cpu_count() or 1
-    times, counts = [], []
-    kw = cycle_kw(args.cycle)
+    times, counts, rr = [], [], None
     for it in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        phi, cnt, rr = c_oracle.solve((g,) * args.dim, p["phi0"], p["rhs"], p["lam"],
-                                      tuple(p[k] for k in coeff_names(args.dim)), stop="residual", rtol=RTOL,
-                                      nthreads=nthreads, **kw)
+        _, cnt, rr = c_oracle.solve((g,) * args.dim, p["phi0"], p["rhs"], p["lam"],
+                                    tuple(p[k] for k in coeff_names(args.dim)), stop="residual", rtol=RTOL,
+                                    nthreads=nthreads, **kw)
         dt = (time.perf_counter() - t0) * 1e3
         if it >= args.warmup:
             times.append(dt)
@@ -191,7 +230,7 @@ def reference_arm(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded GRF coefficients, manufactured rhs)", "impl": "reference",
-        "config": {"workload": workload_name(args),
+        "config": {"workload": workload_name(args.dim, args.m),
                    "cycle": args.cycle, "stop": f"rel. residual <= {RTOL}", "cycles": counts[-1]},
         "cpu_baseline": {"value": ms, "unit": "ms", "cores": nthreads, "kind": "port",
                          "sample": f"{args.steps} full solves (median), C/OpenMP restatement of the reference "
@@ -200,6 +239,22 @@ def reference_arm(args):
         "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "final_rel_residual": rr,
     }
+    if args.workload == "2d" and not args.no_3d:
+        # the 3D half of the metric: one full solve (about 25 s on 16 cores)
+        dim3, m3, cyc3 = WORKLOADS["3d"]
+        from jsolver_gb300 import workloads
+        p3 = workloads.random_3d(m3, seed=args.seed)
+        ms3, n3, c3, rr3, _ = cpu_full_solves(p3, dim3, m3, cycle_kw(cyc3), 1, 0.0)
+        line["workload_3d"] = {
+            "metric": metric_name(dim3, m3), "value": ms3, "unit": "ms", "steps": n3, "warmup": 0,
+            "config": {"workload": workload_name(dim3, m3), "cycle": cyc3, "stop": f"rel. residual <= {RTOL}",
+                       "cycles": c3},
+            "cpu_baseline": {"value": ms3, "unit": "ms", "cores": nthreads, "kind": "port",
+                             "sample": f"{n3} full solve, C/OpenMP restatement (oracle/jmg_oracle.c), "
+                                       f"{nthreads} threads"},
+            "e2e": {"value": ms3, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "final_rel_residual": rr3,
+        }
     print(json.dumps(line), flush=True)
 
 
@@ -217,32 +272,8 @@ def replica_seed(seed, rank):
     return seed + rank
 
 
-def workload_name(args):
-    shape = "^".join([str(args.m + 3), str(args.dim)])
-    return f"{args.dim}d-{args.m}^{args.dim}-random-coeff (arrays {shape} float64)"
-
-
-def cpu_baseline(p, dim, m, cycles_needed, kw, budget_s=20.0):
-    """Time the C oracle on the host cores: a bounded number of cycles, scaled to a solve."""
-    from oracle import c_oracle
-    from oracle.grid import OracleGrid1D
-    g = OracleGrid1D(m)
-    nthreads = os.cpu_count() or 1
-    args = ((g,) * dim, p["phi0"], p["rhs"], p["lam"], tuple(p[k] for k in coeff_names(dim)))
-    t0 = time.perf_counter()
-    c_oracle.solve(*args, fixed=True, max_iters_outer=1, nthreads=nthreads, **kw)
-    t1 = time.perf_counter() - t0
-    n2 = int(max(2, min(cycles_needed, (budget_s - t1) / max(t1 * 0.8, 1e-3))))
-    t0 = time.perf_counter()
-    c_oracle.solve(*args, fixed=True, max_iters_outer=n2, nthreads=nthreads, **kw)
-    t2 = time.perf_counter() - t0
-    per_cycle = max((t2 - t1) / (n2 - 1), 1e-9)
-    setup = max(t1 - per_cycle, 0.0)
-    est = (setup + per_cycle * cycles_needed) * 1e3
-    return {"value": est, "unit": "ms", "cores": nthreads, "kind": "port",
-            "sample": f"C/OpenMP restatement (oracle/jmg_oracle.c): 1 and {n2} fixed cycles timed at full size "
-                      f"({setup * 1e3:.0f} ms set-up + {per_cycle * 1e3:.1f} ms/cycle), scaled to the "
-                      f"{cycles_needed} cycles a solve to 1e-10 takes"}
+def workload_name(dim, m):
+    return f"{dim}d-{m}^{dim}-random-coeff (arrays {m + 3}^{dim} float64)"
 
 
 def adjoint_bench(args):
@@ -367,32 +398,66 @@ def batch_bench(args):
     print(json.dumps(line), flush=True)
 
 
-def main():
-    args = parse()
-    if args.workload == "adjoint":
-        return adjoint_bench(args)
-    if args.workload == "batch":
-        return batch_bench(args)
-    if args.impl == "reference":
-        return reference_arm(args)
+def load_json(name):
+    try:
+        with open(os.path.join(ROOT, *name.split("/"))) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def level_points(dim, m, levels):
+    return [(((m >> l) + 3) ** dim) for l in range(levels)]
+
+
+def coarse_alg_bytes(dim, m, levels, start, gamma, nu1, nu2, elem):
+    """Algorithmic bytes of one coarse sub-cycle launch (a plain cycle from `start` down to
+    the deepest level, L-2): per sweep (d+4)*s*N (phi, rhs, d faces, 1/A_cc read; phi
+    written), per defect + restriction (d+3)*s*N + s*N_c, per prolongation 2*s*N + s*N_c,
+    summed over the recursion's visits (solver_2d.py:582-614)."""
+    N = level_points(dim, m, levels)
+    last = levels - 2
+    sweep = lambda l: (dim + 4) * elem * N[l]  # noqa: E731
+
+    def cyc(l):
+        if l == last:
+            return (nu1 + nu2) * sweep(l)
+        return (nu1 + nu2) * sweep(l) + (dim + 3) * elem * N[l] + 2 * elem * N[l + 1] + 2 * elem * N[l] + \
+            gamma * cyc(l + 1)
+    return cyc(start)
+
+
+def timed_alone(fn, stream, flush, n):
+    """Mean CUDA-event time (ms) of fn(stream) over n launches, L2 flushed before each."""
+    import torch
+    evs = []
+    for _ in range(n):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn(stream)
+        e1.record(stream)
+        evs.append((e0, e1))
+    stream.synchronize()
+    return float(np.mean([a.elapsed_time(b) for a, b in evs]))
+
+
+def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, dev, learned_cmp_on=True):
+    """One workload's line: the form's solve (value, e2e), the plain FP64 comparison, the
+    roofline of the dominant kernel and of the fine sweep, and the CPU baseline."""
     import torch
     import torch.distributed as dist
-    ws_n, rank, local = dist_env()
-    if ws_n > 1:
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    from jsolver_gb300 import _engine, _lib
+    from jsolver_gb300 import _engine, _lib, workloads
     from jsolver_gb300.grid_1d import grid_1D
     from jsolver_gb300.solver_2d import solve_2d
     from jsolver_gb300.solver_3d import solve_3d
 
-    m, dim = args.m, args.dim
     cn = coeff_names(dim)
-    p = make_problem(args, replica_seed(args.seed, rank))
+    seed = replica_seed(args.seed, rank)
+    p = workloads.random_2d(m, seed=seed) if dim == 2 else workloads.random_3d(m, seed=seed)
     g = grid_1D(m)
-    kw = cycle_kw(args.cycle)
-    learned = args.form.startswith("learned")
+    kw = cycle_kw(cycle)
+    learned = args.form.startswith("learned") and dim == 2
     precision = "mixed" if args.form in ("mixed", "learned-mixed") else "fp64"
     opts = dict(stop="residual", rtol=RTOL, precision=precision, max_iters_outer=20000, outer=args.outer, **kw)
     if precision == "mixed":
@@ -428,15 +493,15 @@ def main():
                                  vp(out.data_ptr()), vp(count.data_ptr()), vp(ws.data_ptr()),
                                  ctypes.c_size_t(ws.numel()), vp(s.cuda_stream)))
 
-    def timed(fn, steps, clocks=None):
-        for _ in range(args.warmup):
+    def timed(fn, n_steps, n_warm):
+        for _ in range(n_warm):
             fn(stream)
         stream.synchronize()
         if ws_n > 1:
             dist.barrier()
         torch.cuda.synchronize()
         evs = []
-        for _ in range(steps):
+        for _ in range(n_steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
@@ -464,13 +529,13 @@ def main():
                                                                 outer="richardson")))
             ws64 = torch.empty(plan64.workspace_bytes, dtype=torch.uint8, device=dev)
             f64 = lambda s: solve_dev(s, plan64, ws64, False)  # noqa: E731
-            ms64 = timed(f64, args.steps)
-            plain = {"ms": ms64, "cycles": int(count.item()), "final_rel_residual": rel_residual(plan64, ws64)}
+            ms64 = timed(f64, plain_steps, max(3, min(warmup, 3)))
+            plain = {"ms": ms64, "cycles": int(count.item()), "final_rel_residual": rel_residual(plan64, ws64),
+                     "steps": plain_steps}
             del ws64
         with Clocks(local) as clk:
-            ms = timed(solve_dev, args.steps)
+            ms = timed(solve_dev, steps, warmup)
         cycles = int(count.item())
-        # relative residual of the result, FP64 on the device
         rel_res = rel_residual(plan, wsb)
         guess_rel_res = None
         if learned:
@@ -482,42 +547,64 @@ def main():
         # the metric's other pairing, learned guess + the same form, timed the same way (2D:
         # the network is 2D); its guess is computed inside every timed solve
         learned_cmp = None
-        if not args.no_compare and dim == 2 and not learned:
+        if learned_cmp_on and not args.no_compare and dim == 2 and not learned:
             from jsolver_gb300.learned import GuessNet, WEIGHTS
             if os.path.exists(WEIGHTS):
                 net = GuessNet.load(WEIGHTS, device=dev)
-                ms_l = timed(lambda s_: solve_dev(s_, plan, wsb, True), args.steps)
+                ms_l = timed(lambda s_: solve_dev(s_, plan, wsb, True), steps, warmup)
                 learned_cmp = {"form": f"learned guess + {args.form}", "ms": ms_l,
                                "cycles": int(count.item()) * (args.inner_cycles if precision == "mixed" else 1),
                                "final_rel_residual": rel_residual(plan, wsb),
-                               "speedup_vs_plain_fp64": (plain["ms"] / ms_l) if plain else None}
+                               "speedup_vs_plain_fp64": (plain["ms"] / ms_l) if plain else None,
+                               "gain_vs_zero_guess": ms / ms_l}
+                solve_dev(stream, plan, wsb, False)  # leave the zero-guess form's arrays in the workspace
 
-        # the fine-level red-black sweep of the form's cycles (FP64, or FP32 in the mixed
-        # forms; one launch per sweep where the level sweeps in one pass, else two colour
-        # launches), timed alone with CUDA events on its stream, L2 flushed before every
-        # timed interval. One-pass sweeps alternate two buffers, so they run in pairs.
-        nsw = 20
-        smooth = lib.jmg_op_smooth32_ws if precision == "mixed" else lib.jmg_op_smooth_ws
-        elem = 4 if precision == "mixed" else 8
-        launches_per_sweep = lib.jmg_plan_sweep_launches(plan.handle, 0, 1 if precision == "mixed" else 0)
+        # The fine-level red-black sweep of the form's cycles (FP64, or FP32 in the mixed
+        # forms; one launch per sweep where the level sweeps in one pass, else colour
+        # launches) and the coarse sub-cycle, each timed alone with CUDA events on its
+        # stream, L2 flushed before every timed interval. One-pass sweeps alternate two
+        # buffers, so they run in pairs.
+        fp32 = 1 if precision == "mixed" else 0
+        elem = 4 if fp32 else 8
+        smooth = lib.jmg_op_smooth32_ws if fp32 else lib.jmg_op_smooth_ws
+        launches_per_sweep = lib.jmg_plan_sweep_launches(plan.handle, 0, fp32)
         per = 2 if launches_per_sweep == 1 else 1
-        _lib.check(smooth(plan.handle, 0, 2 * per, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()),
-                          vp(stream.cuda_stream)))
-        sw = []
-        for _ in range(nsw):
-            flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            _lib.check(smooth(plan.handle, 0, per, vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()),
-                              vp(stream.cuda_stream)))
-            e1.record(stream)
-            sw.append((e0, e1))
-        stream.synchronize()
-        sweep_ms = float(np.mean([a.elapsed_time(b) for a, b in sw])) / per
+        wsa = (vp(wsb.data_ptr()), ctypes.c_size_t(wsb.numel()))
+        _lib.check(smooth(plan.handle, 0, 2 * per, *wsa, vp(stream.cuda_stream)))
+        sweep_ms = timed_alone(lambda s_: _lib.check(smooth(plan.handle, 0, per, *wsa, vp(s_.cuda_stream))),
+                               stream, flush, 20) / per
         n0 = (m + 3) ** dim
-        alg_bytes_sweep = (dim + 4) * elem * n0  # (d+4)*s*N0: phi, rhs, d faces, 1/A_cc read; phi written
-        launch_ms = sweep_ms / launches_per_sweep
-        achieved = alg_bytes_sweep / (sweep_ms * 1e-3) / 1e9
+        alg_sweep = (dim + 4) * elem * n0  # (d+4)*s*N0: phi, rhs, d faces, 1/A_cc read; phi written
+        traffic = load_json("profiles/traffic.json").get(
+            f"sweep_{'fp32' if fp32 else 'fp64'}_{dim}d_{m}" + ("_onepass" if launches_per_sweep == 1 else ""))
+        peaks = load_json("MEASURED_PEAKS.json")
+        peak = float(peaks.get("hbm_gbs", 6800.0))
+        peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+        sweep_kernel = (f"{'k_sweep_fused3d' if dim == 3 else 'k_sweep_onepass2d'}<{'float' if fp32 else 'double'}> "
+                        "(fine level; one launch per sweep)" if launches_per_sweep == 1 else
+                        f"k_sweep_color{dim}d<{'float' if fp32 else 'double'}> (fine level; "
+                        f"{launches_per_sweep} launches per sweep)")
+        roof_sweep = {"bound": "hbm", "kernel": sweep_kernel,
+                      "achieved": alg_sweep / launches_per_sweep / (sweep_ms / launches_per_sweep * 1e-3) / 1e9,
+                      "peak": peak, "unit": "GB/s", "peak_source": peak_src,
+                      "alg_bytes_per_launch": alg_sweep / launches_per_sweep,
+                      "launch_ms": sweep_ms / launches_per_sweep, "traffic": traffic}
+        roof_sweep["frac"] = roof_sweep["achieved"] / peak
+        # the coarse sub-cycle (one launch from the first coarse level down)
+        lib.jmg_op_coarse_ws(plan.handle, fp32, *wsa, vp(stream.cuda_stream))
+        cstart = lib.jmg_plan_coarse_start(plan.handle)
+        coarse_ms = timed_alone(lambda s_: _lib.check(lib.jmg_op_coarse_ws(plan.handle, fp32, *wsa,
+                                                                           vp(s_.cuda_stream))), stream, flush, 20)
+        cf = _engine.make_config(**opts)
+        alg_coarse = coarse_alg_bytes(dim, m, plan.levels, cstart, max(cf.gamma, 1), max(cf.nu1, 0), max(cf.nu2, 0),
+                                      elem)
+        roof_coarse = {"bound": "hbm", "kernel": f"k_coarse_cycle<{'float' if fp32 else 'double'}, {dim}> "
+                                                 f"(1 block: levels {m >> cstart}^{dim} ... {m >> (plan.levels - 2)}"
+                                                 f"^{dim} in one launch; latency-bound, its arrays stay in L2)",
+                       "achieved": alg_coarse / (coarse_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                       "peak_source": peak_src, "alg_bytes_per_launch": alg_coarse, "launch_ms": coarse_ms,
+                       "traffic": None}
+        roof_coarse["frac"] = roof_coarse["achieved"] / peak
 
         # end to end through the public API from pinned host buffers
         host = {k: torch.from_numpy(p[k]).pin_memory() for k in ["phi0", "rhs", "lam"] + cn}
@@ -539,7 +626,7 @@ def main():
             e2e_step()
         stream.synchronize()
         e2e_t = []
-        for _ in range(0 if args.no_e2e else args.steps):
+        for _ in range(0 if args.no_e2e else steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
@@ -553,31 +640,23 @@ def main():
 
     fixed_n, per_cycle = ctypes.c_int64(), ctypes.c_int64()
     lib.jmg_plan_launch_counts(plan.handle, ctypes.byref(fixed_n), ctypes.byref(per_cycle))
-    launches = args.steps * (fixed_n.value + per_cycle.value * cycles + (GUESS_LAUNCHES if learned else 0))
+    launches = steps * (fixed_n.value + per_cycle.value * cycles + (GUESS_LAUNCHES if learned else 0))
 
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except OSError:
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    traffic = None
-    try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get(f"sweep_{'fp32' if elem == 4 else 'fp64'}_{dim}d_{m}"
-                                       + ("_onepass" if launches_per_sweep == 1 else ""))
-    except (OSError, ValueError):
-        pass
+    # the kernel with the largest share of the solve in the committed launch list
+    shares = load_json("profiles/launch_shares.json").get(f"{dim}d_{m}_{args.form}_{args.outer}_{cycle}", {})
+    dominant = "coarse" if shares.get("coarse", 0.0) > shares.get("fine_sweep", 0.0) else "fine_sweep"
+    roof = dict(roof_coarse if dominant == "coarse" else roof_sweep)
+    roof["launch_share"] = shares.get(dominant)
+    roof_other = dict(roof_sweep if dominant == "coarse" else roof_coarse)
+    roof_other["launch_share"] = shares.get("fine_sweep" if dominant == "coarse" else "coarse")
 
     line = {
-        "metric": metric_name(dim, m), "value": ms, "unit": "ms", "n_gpus": ws_n, "steps": args.steps,
-        "warmup": args.warmup,
+        "metric": metric_name(dim, m), "value": ms, "unit": "ms", "n_gpus": ws_n, "steps": steps,
+        "warmup": warmup,
         "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": {"fp64": "f64", "mixed": "f32+f64", "learned": "bf16+f64", "learned-mixed": "bf16+f32+f64"}[args.form],
         "data": "synthetic (seeded GRF coefficients, manufactured rhs; no dataset in the reference)",
-        "config": {"workload": workload_name(args), "cycle": args.cycle,
+        "config": {"workload": workload_name(dim, m), "cycle": cycle,
                    "form": args.form, "stop": f"rel. residual <= {RTOL}",
                    "cycles": cycles * (args.inner_cycles if precision == "mixed" else 1),
                    "inner_cycles": args.inner_cycles if precision == "mixed" else None, "outer": args.outer,
@@ -589,25 +668,43 @@ def main():
         "guess_rel_residual": guess_rel_res,
         "learned_guess_form": learned_cmp,
         "max_err_vs_exact_discrete": err_exact,
-        "roofline": {"bound": "hbm",
-                     "kernel": (f"{'k_sweep_fused3d' if dim == 3 else 'k_sweep_onepass2d'}"
-                                f"<{'float' if elem == 4 else 'double'}> (fine level; one launch per sweep)"
-                                if launches_per_sweep == 1 else
-                                f"k_sweep_color{dim}d<{'float' if elem == 4 else 'double'}> (fine level; "
-                                f"{launches_per_sweep} launches per sweep)"),
-                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_src, "alg_bytes_per_sweep": alg_bytes_sweep,
-                     "alg_bytes_per_launch": alg_bytes_sweep / launches_per_sweep, "launch_ms": launch_ms,
-                     "traffic": traffic},
+        "roofline": roof,
+        "roofline_fine_sweep" if dominant == "coarse" else "roofline_coarse": roof_other,
         "e2e": ({"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
                 if e2e_ms is not None else None),
         "gpu_launches": int(launches),
+        "clocks": clk.summary(),
     }
-    line["clocks"] = clk.summary()
     if rank == 0 and not args.no_cpu_baseline:
-        # the reference's algorithm: plain FP64 cycles from phi0 = 0
-        ref_cycles = plain["cycles"] if plain else cycles
-        line["cpu_baseline"] = cpu_baseline(p, dim, m, ref_cycles, kw)
+        # the reference's algorithm (plain FP64 cycles from phi0 = 0), full solves, median;
+        # 3D 256^3 takes ~25 s per solve on 16 cores, so one solve there
+        line["cpu_baseline"] = cpu_baseline(p, dim, m, kw, runs=3 if dim == 2 else 1, budget_s=20.0)
+    return line
+
+
+def main():
+    args = parse()
+    if args.workload == "adjoint":
+        return adjoint_bench(args)
+    if args.workload == "batch":
+        return batch_bench(args)
+    if args.impl == "reference":
+        return reference_arm(args)
+    import torch
+    import torch.distributed as dist
+    ws_n, rank, local = dist_env()
+    if ws_n > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    line = measure(args, args.dim, args.m, args.cycle, args.steps, args.warmup, args.steps, ws_n, rank, local, dev)
+    if args.workload == "2d" and not args.no_3d:
+        # the 3D half of the metric (3D 256^3, F-cycles, the same form); its plain FP64
+        # comparison (about 1.3 s a solve) is timed over at most 5 steps
+        dim3, m3, cyc3 = WORKLOADS["3d"]
+        torch.cuda.empty_cache()
+        line["workload_3d"] = measure(args, dim3, m3, cyc3, args.steps, args.warmup, min(args.steps, 5), ws_n, rank,
+                                      local, dev, learned_cmp_on=False)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws_n > 1:

@@ -215,6 +215,17 @@ int jmg_op_smooth_ws(JmgPlan* plan, int level, int nsweeps, void* workspace, siz
 int jmg_op_smooth32_ws(JmgPlan* plan, int level, int nsweeps, void* workspace, size_t workspace_bytes,
                        jmg_stream_t stream);
 
+/* The coarse sub-cycle of this plan's cycles alone (the levels from
+ * jmg_plan_coarse_start down to the deepest one, in one launch of the single-block
+ * coarse kernel by default), on the level arrays already in the workspace: the coarse
+ * branch of multigrid_cycle (solver_2d.py:582-614) without copies, for timing it alone.
+ * fp32 != 0: the FP32 arrays of a mixed-precision plan. */
+int jmg_op_coarse_ws(JmgPlan* plan, int fp32, void* workspace, size_t workspace_bytes, jmg_stream_t stream);
+/* First level the coarse sub-cycle takes (valid after the plan's first solve or
+ * jmg_op_coarse_ws on a GPU; before that the single-block rule's choice). No reference
+ * counterpart. */
+int jmg_plan_coarse_start(const JmgPlan* plan);
+
 /* Kernel launches per sweep of a level in this plan's solves (fp32 != 0: the FP32
  * cycles of a mixed plan): 1 for the one-pass 3D sweep, 2 colour passes, 4 sub-lattice
  * passes with D_xy; 0 for a bad level. No reference counterpart. */
@@ -231,12 +242,13 @@ int jmg_plan_launch_counts(const JmgPlan* plan, int64_t* per_solve_fixed, int64_
  * only inputs and outputs, a loop that cannot afford an allocation's synchronisation).
  * No counterpart in the reference. It needs no plan and no workspace: its scratch is a
  * fixed 16 MiB array of this library's device memory, kept on every GPU that loads the
- * library until the process exits, so grids whose level-0 coefficients need more
- * (roughly 2D beyond 512^2, 3D beyond 64^3) are rejected with JMG_ERR_VALUE. The first
- * call on each device looks up the array's address; make it outside stream capture.
- * All calls share the array: calls that overlap on the GPU race, so serialise them.
- * phi, rhs and the coefficient arrays are dense padded device arrays, as for jmg_solve;
- * phi's frame is used as stored (the solver returns phi with a zero frame). */
+ * library until the process exits, so grids whose level-0 phi copy and coefficients
+ * need more (roughly 2D beyond 512^2, 3D beyond 64^3) are rejected with JMG_ERR_VALUE.
+ * The first call on each device looks up the array's address; make it outside stream
+ * capture. All calls share the array: calls that overlap on the GPU race, so serialise
+ * them. phi, rhs and the coefficient arrays are dense padded device arrays, as for
+ * jmg_solve; phi's frame is read as zero, as jmg_rel_residual reads it, so the two give
+ * the same number for any phi. */
 int jmg_rel_residual_noalloc(const JmgGrid* grid, const double* phi, const double* rhs,
                              const JmgCoeffs* coeffs, double* out, jmg_stream_t stream);
 

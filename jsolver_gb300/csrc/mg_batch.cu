@@ -25,7 +25,7 @@ using namespace jmg;
 
 namespace {
 
-constexpr int kMaxLanes = 32;
+constexpr int kMaxLanes = JmgPlan::kMaxLanes;
 
 size_t lane_bytes(const JmgPlan* p) { return align_up(p->ws_bytes); }
 

@@ -731,6 +731,8 @@ __global__ void k_write_i64(long long* out, long long v) { *out = v; }
 
 int jmg::set_error_message(int code, const char* msg) { return set_err(code, "%s", msg); }
 
+int jmg::block_coarse_level(const JmgPlan* p) { return block_coarse_start(p); }
+
 // JMG_PDL=0 turns programmatic dependent launch off (read once per process)
 bool jmg::pdl_enabled() {
   static const bool on = [] {
@@ -1067,6 +1069,31 @@ int jmg_op_smooth32_ws(JmgPlan* p, int level, int nsweeps, void* ws, size_t byte
   JMG_CUDA(cudaGetLastError());
   return JMG_OK;
 }
+
+int jmg_op_coarse_ws(JmgPlan* p, int fp32, void* ws, size_t bytes, jmg_stream_t stream) {
+  int rc = check_ws(p, ws, bytes);
+  if (rc) return rc;
+  if (fp32 && !p->mixed) return set_err(JMG_ERR_VALUE, "jmg_op_coarse_ws(fp32=1) needs a plan with precision mixed");
+  if ((rc = coarse_setup(p))) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  const CycleParams cp = cycle_params(p, p->off_diag);
+  const int lev = p->coarse_start;
+  if (fp32) {
+    LvlTable<float> t = make_table<float>(p, ws);
+    LvlTable<float>* dt = ptr<LvlTable<float>>(ws, p->off_tab32);
+    launch_store_table<float>(t, dt, s);
+    emit_cycle<float>(p, t, dt, cp, lev, false, false, s);
+  } else {
+    LvlTable<double> t = make_table<double>(p, ws);
+    LvlTable<double>* dt = ptr<LvlTable<double>>(ws, p->off_tab64);
+    launch_store_table<double>(t, dt, s);
+    emit_cycle<double>(p, t, dt, cp, lev, false, false, s);
+  }
+  JMG_CUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
+int jmg_plan_coarse_start(const JmgPlan* p) { return p ? p->coarse_start : -1; }
 
 int jmg_plan_sweep_launches(const JmgPlan* p, int level, int fp32) {
   if (!p || level < 0 || level >= p->used) return 0;

@@ -10,9 +10,11 @@
 //
 // The scratch is a file-scope __device__ array of JMG_NOALLOC_SCRATCH_DOUBLES doubles
 // (16 MiB). Every GPU that loads this library keeps it until the process exits. It
-// holds the level-0 stencil coefficients (x/y(/z) face couplings, A_cc and 1/A_cc, in
-// the dense padded layout of the inputs), the per-block partial sums and the two norms.
-// Grids whose coefficients do not fit are rejected with JMG_ERR_VALUE and a message
+// holds a copy of phi with its frame set to zero (jmg_rel_residual copies phi into its
+// workspace the same way, so a phi whose frame is not zero gives the same number in
+// both; rhs is read at interior points only and needs no copy), the level-0 stencil
+// coefficients (x/y(/z) face couplings, A_cc and 1/A_cc), all in the dense padded layout
+// of the inputs, the per-block partial sums and the two norms. Grids whose arrays do not fit are rejected with JMG_ERR_VALUE and a message
 // stating the limit.
 //
 // Host code cannot pass the array's name to a kernel (on the host that name is only a
@@ -71,8 +73,9 @@ int scratch_for_current_device(double** out) {
 extern "C" {
 
 // Relative residual ||rhs - L_h phi||_2 / ||rhs||_2 over the interior indices 2..m of
-// level 0, in FP64, written to the device double *out. Same arithmetic as
-// jmg_rel_residual, without a workspace. See the file header for the scratch rules.
+// level 0, in FP64, written to the device double *out. Same kernels and the same number
+// as jmg_rel_residual (phi's frame is read as zero in both), without a workspace. See the
+// file header for the scratch rules.
 int jmg_rel_residual_noalloc(const JmgGrid* grid, const double* phi, const double* rhs, const JmgCoeffs* coeffs,
                              double* out, jmg_stream_t stream) {
   if (!grid || !phi || !rhs || !coeffs || !out) return noalloc_err(JMG_ERR_VALUE, "NULL argument");
@@ -85,6 +88,7 @@ int jmg_rel_residual_noalloc(const JmgGrid* grid, const double* phi, const doubl
     if (coeffs->D[a] == nullptr) ++nscalar;
   if (nscalar != 0 && nscalar != dim)
     return noalloc_err(JMG_ERR_VALUE, "Shape mismatch: the D components must be all scalars or all arrays.");
+  if (coeffs->D_xy && dim == 3) return noalloc_err(JMG_ERR_VALUE, "D_xy is a 2D argument");
   if (coeffs->D_xy && nscalar == 0)
     return noalloc_err(JMG_ERR_VALUE, "jmg_rel_residual_noalloc takes no D_xy: its fixed scratch holds the "
                                       "5-point coefficients only; use jmg_rel_residual");
@@ -100,7 +104,8 @@ int jmg_rel_residual_noalloc(const JmgGrid* grid, const double* phi, const doubl
   const unsigned long long n_al = (n + 31) / 32 * 32;  // keep every array 256-byte aligned
   const int nparts = residual_num_parts(dim, b);
   const unsigned long long state_doubles = (sizeof(LoopState) + 255) / 256 * 32;
-  const unsigned long long need = (unsigned long long)(dim + 2) * n_al + (unsigned long long)(nparts + 31) / 32 * 32 +
+  // phi with a zero frame, dim face arrays, A_cc, 1/A_cc; partial sums; loop state
+  const unsigned long long need = (unsigned long long)(dim + 3) * n_al + (unsigned long long)(nparts + 31) / 32 * 32 +
                                   state_doubles;
   if (need > JMG_NOALLOC_SCRATCH_DOUBLES) {
     char msg[256];
@@ -115,12 +120,12 @@ int jmg_rel_residual_noalloc(const JmgGrid* grid, const double* phi, const doubl
   if (rc != JMG_OK) return rc;
 
   Lvl<double> a{};
-  a.phi = const_cast<double*>(phi);
-  a.rhs = const_cast<double*>(rhs);
-  a.wx = scratch;
-  a.wy = scratch + n_al;
-  a.wz = dim == 3 ? scratch + 2 * n_al : nullptr;
-  a.acc = scratch + (dim == 3 ? 3 : 2) * n_al;
+  a.phi = scratch;
+  a.rhs = const_cast<double*>(rhs);  // read at interior points only
+  a.wx = scratch + n_al;
+  a.wy = scratch + 2 * n_al;
+  a.wz = dim == 3 ? scratch + 3 * n_al : nullptr;
+  a.acc = scratch + (dim == 3 ? 4 : 3) * n_al;
   a.invd = a.acc + n_al;
   double* parts = a.invd + n_al;
   LoopState* st = reinterpret_cast<LoopState*>(parts + (nparts + 31) / 32 * 32);
@@ -146,6 +151,9 @@ int jmg_rel_residual_noalloc(const JmgGrid* grid, const double* phi, const doubl
   }
 
   cudaStream_t s = (cudaStream_t)stream;
+  // phi with a zero frame, as jmg_rel_residual copies it (the defect at i = 2 and i = m
+  // reads phi at the frame indices 1 and m + 1)
+  launch_copy_in(b, phi, a.phi, 1, s);
   // level-0 coefficients over the whole box (every scratch value read below is written here)
   launch_hierarchy_level(dim, 0, a, b, b, in, idl, sq, nullptr, nullptr, b, s);
   launch_residual_partials<double>(dim, a, nullptr, parts, nparts, s);

@@ -48,7 +48,10 @@ struct JmgPlan {
     void* ws;
     cudaGraphExec_t exec;
   };
-  static constexpr int kMaxGraphs = 32;
+  // more than the 32 lanes of a batched solve, so that a full batch alternating with
+  // single solves on other workspaces keeps every lane's graph
+  static constexpr int kMaxLanes = 32;
+  static constexpr int kMaxGraphs = kMaxLanes + 8;
   std::vector<GraphSlot> graphs;
   cudaStream_t cap = nullptr;
   // batched solves: the lanes' streams and the events that fork them from and join them
@@ -95,5 +98,8 @@ int check_ws(const JmgPlan* p, void* ws, size_t bytes);
 int build_hierarchy(JmgPlan* p, const JmgCoeffs* c, void* ws, cudaStream_t s);
 // chooses the coarse sub-cycle kernel once per plan (needs the GPU; mg_driver.cu)
 int coarse_setup(JmgPlan* p);
+// first level the single-block coarse kernel takes (at most JMG_COARSE_POINTS padded
+// points, 2048 by default; mg_driver.cu)
+int block_coarse_level(const JmgPlan* p);
 
 }  // namespace jmg

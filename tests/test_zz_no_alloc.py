@@ -6,7 +6,9 @@ cannot afford the synchronisation an allocation may cause. For them the library 
 jmg_rel_residual_noalloc, whose scratch is a fixed array of the library's own device
 memory instead of a caller workspace. This test calls it through the C ABI and checks it
 against jmg_rel_residual (which uses a caller workspace) on consecutive calls with
-different grids, so a call that read stale scratch from the previous one would fail.
+different grids and coefficient forms (arrays and scalars, a phi with a nonzero frame, a
+3D grid large enough for the wide reduction), so a call that read stale scratch from the
+previous one would fail.
 This file is collected last on purpose.
 """
 import ctypes
@@ -51,12 +53,37 @@ def _problem(dim, m, seed, cycles):
 
 
 def _coeffs(lam, D):
-    keep = [_dev(lam)] + [_dev(d) for d in D]
+    """JmgCoeffs over device copies; a Python float selects the scalar form."""
+    keep = []
     co = _lib.JmgCoeffs()
-    co.lam = keep[0].data_ptr()
-    for k, t in enumerate(keep[1:]):
-        co.D[k] = t.data_ptr()
+    if np.ndim(lam) == 0:
+        co.lam, co.lam_scalar = None, float(lam)
+    else:
+        keep.append(_dev(lam))
+        co.lam = keep[-1].data_ptr()
+    for k, d in enumerate(D):
+        if np.ndim(d) == 0:
+            co.D[k], co.D_scalar[k] = None, float(d)
+        else:
+            keep.append(_dev(d))
+            co.D[k] = keep[-1].data_ptr()
     return co, keep
+
+
+def _random_case(ms, seed, scalar_D=False, scalar_lam=False, frame=False):
+    """Random phi and rhs (a nontrivial residual) on grids of resolutions ms = (mx, my[, mz]);
+    with frame=True, the frames of phi and rhs hold random values too (both entry points
+    read phi's frame as 0 and rhs at interior points only)."""
+    rng = np.random.default_rng(seed)
+    shape = tuple(m + 3 for m in reversed(ms))
+    phi = rng.standard_normal(shape)
+    rhs = rng.standard_normal(shape)
+    if not frame:
+        phi, rhs = W._zero_frame(phi), W._zero_frame(rhs)
+    D = tuple(1.0 + 0.5 * k for k in range(len(ms))) if scalar_D else \
+        tuple(np.exp(rng.standard_normal(shape)) for _ in ms)
+    lam = 0.75 if scalar_lam else rng.uniform(0.0, 5.0, shape)
+    return tuple(grid_1D(m) for m in ms), phi, rhs, lam, D
 
 
 def _with_workspace(grids, phi, rhs, co):
@@ -84,19 +111,50 @@ def _no_alloc(grids, phi, rhs, co):
 
 
 def test_no_alloc_matches_workspace_version_on_consecutive_calls():
-    cases = [(2, 256, 1, 3), (3, 32, 2, 2), (2, 64, 3, 1), (2, 256, 1, 3)]
+    """Consecutive calls on different grids and coefficient forms share the one scratch
+    array; each must match jmg_rel_residual, and repeating the first call must give the
+    same bits after the others have overwritten the scratch."""
+    cases = [
+        lambda: _problem(2, 256, 1, 3),                                   # array lam and D
+        lambda: _problem(3, 32, 2, 2),
+        lambda: _random_case((64, 64), 3, scalar_D=True),                # scalar D, array lam
+        lambda: _random_case((128, 64), 4, scalar_lam=True),             # array D, scalar lam
+        lambda: _random_case((16, 32, 16), 5, scalar_D=True, scalar_lam=True),
+        lambda: _random_case((32, 32, 32), 6, scalar_D=True),
+        lambda: _random_case((256, 256), 7, frame=True),                 # phi's frame is not zero
+        lambda: _random_case((16, 16, 32), 8, frame=True, scalar_lam=True),
+        lambda: _random_case((32, 128, 64), 9),  # 127 x 63 = 8001 interior rows: 1216 partial sums
+        lambda: _problem(2, 256, 1, 3),
+    ]
     results = []
-    for dim, m, seed, cycles in cases:
-        grids, phi, rhs, lam, D = _problem(dim, m, seed, cycles)
+    for make in cases:
+        grids, phi, rhs, lam, D = make()
         co, keep = _coeffs(lam, D)
         phi_d, rhs_d = _dev(phi), _dev(rhs)
         want = _with_workspace(grids, phi_d, rhs_d, co)
         got = _no_alloc(grids, phi_d, rhs_d, co)
         assert np.isfinite(got) and want > 0
-        assert abs(got - want) <= TOL * want, (dim, m, got, want)
+        assert abs(got - want) <= TOL * want, ([g.mx for g in grids], got, want)
         results.append(got)
     # the repeated first case gives the same value after other grids used the scratch
-    assert results[0] == results[3]
+    assert results[0] == results[-1]
+
+
+def test_no_alloc_rejects_d_xy_in_3d():
+    lib = _lib.load()
+    g = grid_1D(8)
+    grid = _engine.make_grid((g, g, g))
+    x = torch.zeros((11, 11, 11), dtype=torch.float64, device=DEV)
+    co = _lib.JmgCoeffs()
+    for k in range(3):
+        co.D[k] = x.data_ptr()
+    co.lam = x.data_ptr()
+    co.D_xy = x.data_ptr()
+    out = torch.zeros((), dtype=torch.float64, device=DEV)
+    rc = lib.jmg_rel_residual_noalloc(ctypes.byref(grid), vp(x.data_ptr()), vp(x.data_ptr()), ctypes.byref(co),
+                                      vp(out.data_ptr()), vp(torch.cuda.current_stream().cuda_stream))
+    assert rc == _lib.JMG_ERR_VALUE
+    assert b"D_xy is a 2D argument" in lib.jmg_last_error()
 
 
 def test_no_alloc_rejects_grids_beyond_its_scratch():
