@@ -193,13 +193,24 @@ int jmg_solve_fixed_vjp(JmgPlan* plan, const double* phi0, const double* rhs, co
                         double* Dxx_bar, double* Dyy_bar, void* workspace, size_t workspace_bytes,
                         void* adjoint_workspace, size_t adjoint_workspace_bytes, jmg_stream_t stream);
 
-/* Forward mode of the fixed-mode 2D solve (jax.jvp through solve_2d with fixed=True,
- * solver_2d.py:461-463): phi and its tangent phi_dot for tangents phi0_dot, rhs_dot and
- * the coefficient tangents coeffs_dot (lam, D_xx, D_yy; arrays where coeffs has arrays,
- * scalars where it has scalars). FP64, 5-point stencil, the reference's iteration.
- * tangent_workspace (jmg_tangent_workspace_bytes, the plan's workspace size) holds the
- * tangent arrays in the plan's layout. */
+/* Forward mode of the solve (jax.jvp through solve_2d / solve_3d: through the fixed
+ * fori_loop, solver_2d.py:461-463, and through the dynamic while_loop, solver_2d.py:465-477,
+ * whose cycle count follows the primal's distance test and is not differentiated; the same
+ * in solver_3d.py:468-477). Writes phi and its tangent phi_dot for the tangents phi0_dot,
+ * rhs_dot and the coefficient tangents coeffs_dot (lam, D components and, with a plan
+ * created with off_diag, D_xy: arrays where coeffs has arrays, scalars where it has
+ * scalars). 2D and 3D, 5-, 7- and 9-point stencils, V/W/F cycles, skip_pre, any nu1/nu2;
+ * the reference's FP64 iteration (precision fp64, outer richardson) with fixed = 1 or the
+ * distance stop. phi and the cycle count equal jmg_solve's bit for bit. count_out: device
+ * int64 or NULL. The dynamic loop reads the device's loop decision back after every cycle.
+ * tangent_workspace: jmg_tangent_workspace_bytes(plan) bytes, 256-byte aligned (the
+ * tangent coefficient hierarchy and the dual-number level arrays). */
 size_t jmg_tangent_workspace_bytes(const JmgPlan* plan);
+int jmg_solve_jvp(JmgPlan* plan, const double* phi0, const double* rhs, const JmgCoeffs* coeffs,
+                  const double* phi0_dot, const double* rhs_dot, const JmgCoeffs* coeffs_dot, double* phi_out,
+                  double* phi_dot_out, int64_t* count_out, void* workspace, size_t workspace_bytes,
+                  void* tangent_workspace, size_t tangent_workspace_bytes, jmg_stream_t stream);
+/* jmg_solve_jvp for a plan with fixed = 1 (no count output). */
 int jmg_solve_fixed_jvp(JmgPlan* plan, const double* phi0, const double* rhs, const JmgCoeffs* coeffs,
                         const double* phi0_dot, const double* rhs_dot, const JmgCoeffs* coeffs_dot,
                         double* phi_out, double* phi_dot_out, void* workspace, size_t workspace_bytes,

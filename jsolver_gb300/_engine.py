@@ -180,8 +180,19 @@ def solve(grids, phi, rhs, lam, D, D_xy=None, guess=None, **opts):
     cfg = make_config(off_diag=off, **opts)
     plan = CACHE.plan(grid, cfg)
     torch_in = any(is_cuda_tensor(a) for a in [phi, rhs, lam] + list(D))
-    wants_grad = torch.is_grad_enabled() and any(isinstance(a, torch.Tensor) and a.requires_grad
-                                                 for a in [phi, rhs, lam] + list(D))
+    args = [phi, rhs, lam] + list(D) + ([] if D_xy is None else [D_xy])
+    from .adjoint import has_forward_tangent
+    if any(has_forward_tangent(a) for a in args):
+        # forward mode (torch.func.jvp / forward_ad): jax.jvp of the reference's solve
+        if guess is not None:
+            raise ValueError("guess= is available for 2D solves without gradients")
+        if cfg.precision != _lib.PREC_FP64 or cfg.outer != _lib.OUTER_RICHARDSON or \
+                (not cfg.fixed and cfg.stop != _lib.STOP_DISTANCE):
+            raise NotImplementedError("forward mode differentiates the reference's FP64 iteration (fixed count or "
+                                      "the distance stop)")
+        from .adjoint import solve_forward_ad
+        return solve_forward_ad(grids, phi, rhs, lam, D, D_xy, **opts)
+    wants_grad = torch.is_grad_enabled() and any(isinstance(a, torch.Tensor) and a.requires_grad for a in args)
     if guess is not None and (ndim != 2 or wants_grad):
         raise ValueError("guess= is available for 2D solves without gradients")
     if wants_grad:

@@ -74,6 +74,8 @@ _SIGS = {
     "jmg_tangent_workspace_bytes": (ctypes.c_size_t, [_P]),
     "jmg_solve_fixed_jvp": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(JmgCoeffs), _P, _P, ctypes.POINTER(JmgCoeffs), _P,
                                            _P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, _P]),
+    "jmg_solve_jvp": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(JmgCoeffs), _P, _P, ctypes.POINTER(JmgCoeffs), _P, _P,
+                                     _P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, _P]),
     "jmg_solve_fixed_vjp": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(JmgCoeffs), _P, _P, _P, _P, _P, _P, _P,
                                            ctypes.c_size_t, _P, ctypes.c_size_t, _P]),
     "jmg_net_num_params": (ctypes.c_int64, []),

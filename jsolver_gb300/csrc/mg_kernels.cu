@@ -15,6 +15,7 @@
 #include "mg_block.cuh"
 #include "mg_common.cuh"
 #include "mg_kernels.h"
+#include "mg_dual.cuh"
 
 namespace jmg {
 
@@ -344,6 +345,19 @@ void launch_restrict(int dim, const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s) 
   }
 }
 
+// Defect + restriction with one thread per coarse point (the grid form of launch_restrict
+// in 2D and 3D; the tiled forms give the same bits for FP64 and FP32).
+template <typename T>
+void launch_restrict_grid(int dim, const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s) {
+  if (dim == 2) {
+    dim3 b(32, 8), g(cdiv(c.mx + 3, 32), cdiv(c.my + 3, 8));
+    launch_k(k_restrict2d<T>, g, b, 0, s, f, c);
+  } else {
+    dim3 b(32, 8, 1), g(cdiv(c.mx + 3, 32), cdiv(c.my + 3, 8), c.mz + 3);
+    launch_k(k_restrict3d<T>, g, b, 0, s, f, c);
+  }
+}
+
 template <typename T>
 void launch_prolong(int dim, const Lvl<T>& f, const Lvl<T>& c, int diag, cudaStream_t s) {
   if (dim == 2) {
@@ -391,5 +405,11 @@ void launch_store_table(const LvlTable<T>& tab, LvlTable<T>* dst, cudaStream_t s
 JMG_INST(double)
 JMG_INST(float)
 #undef JMG_INST
+template void launch_restrict_grid<double>(int, const Lvl<double>&, const Lvl<double>&, cudaStream_t);
+// the forward-mode solve (mg_tangent.cu): the same kernels over dual numbers
+template void launch_sweep<Dual>(int, Lvl<Dual>&, cudaStream_t, bool);
+template void launch_restrict_grid<Dual>(int, const Lvl<Dual>&, const Lvl<Dual>&, cudaStream_t);
+template void launch_coarse_cycle<Dual>(int, const LvlTable<Dual>*, const CycleParams&, int, int, int, cudaStream_t);
+template void launch_store_table<Dual>(const LvlTable<Dual>&, LvlTable<Dual>*, cudaStream_t);
 
 }  // namespace jmg

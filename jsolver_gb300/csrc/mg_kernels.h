@@ -64,6 +64,8 @@ template <typename T> void launch_restrict_tile2d(const Lvl<T>& f, const Lvl<T>&
 int residual_f32_parts2d(int mx, int my);
 void launch_residual_f32_2d(const Lvl<double>& a, float* r32, double* parts, cudaStream_t s);
 template <typename T> void launch_restrict(int dim, const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s);
+// the one-thread-per-coarse-point restriction (2D and 3D)
+template <typename T> void launch_restrict_grid(int dim, const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s);
 template <typename T> void launch_prolong(int dim, const Lvl<T>& f, const Lvl<T>& c, int diag, cudaStream_t s);
 template <typename T>
 void launch_coarse_cycle(int dim, const LvlTable<T>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,

@@ -1,29 +1,37 @@
-// mg_tangent.cu — forward mode of the fixed-mode 2D solve (Jacobian-vector product).
+// mg_tangent.cu — forward mode of the solve (Jacobian-vector product), 2D and 3D, fixed
+// and dynamic, 5-, 7- and 9-point stencils.
 //
-// The reference gets forward-mode derivatives from jax.jvp through its fixed loop
-// (solver_2d.py:461-463). Here every quantity carries its tangent. The coefficient
-// hierarchy (solver_2d.py:326-421) is linear in (lambda, D) except 1/A_cc, so the tangent
-// hierarchy is the same hierarchy built from the tangent coefficients, with d(1/A_cc) =
-// -(1/A_cc)^2 d(A_cc) replacing the reciprocal. The cycle is affine in (phi, rhs) for
-// fixed coefficients; its tangent runs the same schedule with dual-number kernels:
-//   sweep     phi' = (s - rhs) / A_cc,   s = sum of couplings x neighbours
-//             dphi' = (ds - drhs) / A_cc + (s - rhs) d(1/A_cc),
-//             ds = sum of (dcoupling x neighbour + coupling x dneighbour)
-//   defect    d = A_cc phi - sum + rhs,  dd = dA_cc phi + A_cc dphi - dsum + drhs
-//   restrict  linear in the defects (same weights for both)
-//   prolong   linear (the grid-wide kernel applied to the tangent arrays)
-// The tangent arrays live in a second workspace with the plan's own layout. Every level
-// runs grid-wide kernels here (no single-block coarse kernel): the tangent is a test and
-// analysis path, not the solver's hot loop.
+// The reference gets forward-mode derivatives from jax.jvp through its solve: through the
+// fixed fori_loop (solver_2d.py:461-463) and through the dynamic while_loop (465-477),
+// whose cycle count is not differentiated: the loop runs as many cycles as the primal's
+// distance test asks for and the tangent rides along (tests/test_solver_2d.py:173-176,
+// tests/test_solver_3d.py:208-211 check it on every problem). Here every quantity is a
+// dual number (mg_dual.cuh) and the cycle runs the solver's own kernels over Duals:
+//   coefficients  the hierarchy (solver_2d.py:326-421, solver_3d.py:338-429) is linear in
+//                 (lambda, D, D_xy) except 1/A_cc, so the tangent hierarchy is the plan's
+//                 hierarchy built from the tangent coefficients, with
+//                 (1/A_cc)' = -(1/A_cc)^2 A_cc'; value and tangent arrays are packed into
+//                 Dual arrays per level;
+//   cycle         colour sweeps (sub-lattice passes with D_xy), the one-thread-per-coarse-
+//                 point restriction, the prolongation by coarse cells and the single-block
+//                 coarse cycle, all instantiated for Dual;
+//   loop          fixed: max_iters_outer cycles; dynamic: the reference's distance test on
+//                 the value part (max |phi_old - phi| over the padded box, NaN ends it),
+//                 decided on the device by the solver's loop kernel and read back by the
+//                 host after every cycle.
+// The value part is the plain FP64 solver's arithmetic, so phi and the cycle count are
+// jmg_solve's bit for bit. The tangent workspace holds the tangent hierarchy in the plan's
+// layout, then the Dual level arrays, the distance snapshot and the loop state.
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "../../include/jmg.h"
+#include "mg_dual.cuh"
 #include "mg_kernels.h"
 #include "mg_plan.h"
 
 namespace jmg {
-
-int set_error_message(int code, const char* msg);
 
 namespace {
 
@@ -31,103 +39,151 @@ int fail(int code, const char* msg) { return set_error_message(code, msg); }
 
 inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
-// d(1/A_cc) = -(1/A_cc)^2 dA_cc over the whole level box (frames: 1/A_cc = 0 there)
-__global__ void k_tan_invd(Lvl<double> a, Lvl<double> t) {
-  const int I = blockIdx.x * blockDim.x + threadIdx.x;
-  const int J = blockIdx.y * blockDim.y + threadIdx.y;
-  if (I > a.mx + 2 || J > a.my + 2) return;
-  const long long p = (long long)J * a.P + I;
-  const double inv = a.invd[p];
-  t.invd[p] = -(inv * inv) * t.acc[p];
+// Dual arrays of a level: phi, rhs, wx, wy, [wz], invd, acc, [A_ll, A_rl, A_lr, A_rr]
+int dual_arrays(const JmgPlan* p) { return (p->dim == 3 ? 7 : 6) + (p->off_diag ? 4 : 0); }
+
+struct TanLayout {
+  std::vector<size_t> lvl;  // first Dual array of every level
+  size_t phi_old = 0;       // FP64 level-0 snapshot of the distance test
+  size_t state = 0;         // LoopState
+  size_t tab = 0;           // LvlTable<Dual> of the coarse kernel
+  size_t total = 0;
+};
+
+TanLayout tan_layout(const JmgPlan* p) {
+  TanLayout L;
+  size_t off = align_up(p->ws_bytes);  // the tangent hierarchy, in the plan's layout
+  auto take = [&](size_t b) {
+    const size_t o = off;
+    off = align_up(off + b);
+    return o;
+  };
+  for (int l = 0; l < p->used; ++l) L.lvl.push_back(take((size_t)dual_arrays(p) * p->lv[l].elems * sizeof(Dual)));
+  L.phi_old = take(p->lv[0].elems * 8);
+  L.state = take(sizeof(LoopState));
+  L.tab = take(sizeof(LvlTable<Dual>));
+  L.total = off;
+  return L;
 }
 
-// one colour of the dual sweep (solver_2d.py:670-692 with tangents)
-__global__ void k_dual_sweep2d(Lvl<double> a, Lvl<double> t, int color) {
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;  // row
-  if (i > a.my) return;
-  const int j = 2 + ((i + color) & 1) + 2 * (blockIdx.x * blockDim.x + threadIdx.x);  // column
-  if (j > a.mx) return;
-  const long long p = (long long)i * a.P + j;
-  const int P = a.P;
-  double s = a.wy[p] * a.phi[p + P];
-  s = fma(a.wy[p - P], a.phi[p - P], s);
-  s = fma(a.wx[p], a.phi[p + 1], s);
-  s = fma(a.wx[p - 1], a.phi[p - 1], s);
-  double ds = t.wy[p] * a.phi[p + P] + a.wy[p] * t.phi[p + P];
-  ds += t.wy[p - P] * a.phi[p - P] + a.wy[p - P] * t.phi[p - P];
-  ds += t.wx[p] * a.phi[p + 1] + a.wx[p] * t.phi[p + 1];
-  ds += t.wx[p - 1] * a.phi[p - 1] + a.wx[p - 1] * t.phi[p - 1];
-  const double r = s - a.rhs[p];
-  a.phi[p] = r * a.invd[p];
-  t.phi[p] = (ds - t.rhs[p]) * a.invd[p] + r * t.invd[p];
-}
-
-__device__ __forceinline__ void dual_defect(const Lvl<double>& a, const Lvl<double>& t, long long p, double* d,
-                                            double* dd) {
-  const int P = a.P;
-  double v = a.acc[p] * a.phi[p];
-  v = fma(-a.wx[p - 1], a.phi[p - 1], v);
-  v = fma(-a.wx[p], a.phi[p + 1], v);
-  v = fma(-a.wy[p - P], a.phi[p - P], v);
-  v = fma(-a.wy[p], a.phi[p + P], v);
-  *d = v + a.rhs[p];
-  double w = t.acc[p] * a.phi[p] + a.acc[p] * t.phi[p];
-  w -= t.wx[p - 1] * a.phi[p - 1] + a.wx[p - 1] * t.phi[p - 1];
-  w -= t.wx[p] * a.phi[p + 1] + a.wx[p] * t.phi[p + 1];
-  w -= t.wy[p - P] * a.phi[p - P] + a.wy[p - P] * t.phi[p - P];
-  w -= t.wy[p] * a.phi[p + P] + a.wy[p] * t.phi[p + P];
-  *dd = w + t.rhs[p];
-}
-
-// coarse rhs and its tangent from the red-point defects (solver_2d.py:616-647); coarse phi
-// and its tangent set to zero, over the full padded coarse box
-__global__ void k_dual_restrict2d(Lvl<double> af, Lvl<double> tf, Lvl<double> ac, Lvl<double> tc) {
-  const int I = blockIdx.x * blockDim.x + threadIdx.x;
-  const int J = blockIdx.y * blockDim.y + threadIdx.y;
-  if (I > ac.mx + 2 || J > ac.my + 2) return;
-  const long long q = (long long)J * ac.P + I;
-  double v = 0.0, dv = 0.0;
-  if (J >= 2 && J <= ac.my && I >= 2 && I <= ac.mx) {
-    const int P = af.P;
-    const long long c = (long long)(2 * J - 1) * P + (2 * I - 1);
-    double dne, dnw, dse, dsw, dc, tne, tnw, tse, tsw, tc0;
-    dual_defect(af, tf, c + P + 1, &dne, &tne);
-    dual_defect(af, tf, c + P - 1, &dnw, &tnw);
-    dual_defect(af, tf, c - P + 1, &dse, &tse);
-    dual_defect(af, tf, c - P - 1, &dsw, &tsw);
-    dual_defect(af, tf, c, &dc, &tc0);
-    v = 0.0625 * (((dne + dnw) + dse) + dsw) + 0.25 * dc;
-    dv = 0.0625 * (((tne + tnw) + tse) + tsw) + 0.25 * tc0;
+Lvl<Dual> dual_lvl(const JmgPlan* p, void* tws, const TanLayout& L, int l) {
+  const LevelInfo& li = p->lv[l];
+  const size_t n = li.elems;
+  Dual* b = ptr<Dual>(tws, L.lvl[l]);
+  Lvl<Dual> a{};
+  int k = 0;
+  a.phi = b + n * k++;
+  a.rhs = b + n * k++;
+  a.wx = b + n * k++;
+  a.wy = b + n * k++;
+  a.wz = p->dim == 3 ? b + n * k++ : nullptr;
+  a.invd = b + n * k++;
+  a.acc = b + n * k++;
+  if (p->off_diag) {
+    a.xll = b + n * k++;
+    a.xrl = b + n * k++;
+    a.xlr = b + n * k++;
+    a.xrr = b + n * k++;
   }
-  ac.rhs[q] = v;
-  ac.phi[q] = 0.0;
-  tc.rhs[q] = dv;
-  tc.phi[q] = 0.0;
+  a.mx = li.m[0];
+  a.my = li.m[1];
+  a.mz = li.m[2];
+  a.P = li.box.P;
+  a.S = li.box.S;
+  a.phi2 = nullptr;
+  return a;
 }
 
-void dual_sweep(const Lvl<double>& a, const Lvl<double>& t, cudaStream_t s) {
-  dim3 b(64, 4), g(cdiv(a.mx / 2, 64), cdiv(a.my - 1, 4));
-  for (int c = 0; c < 2; ++c) k_dual_sweep2d<<<g, b, 0, s>>>(a, t, c);
+// out = (v, t) over the pitched box; with invd, out = (v, -v^2 t): t is A_cc' and v 1/A_cc
+__global__ void k_pack_dual(Box b, const double* __restrict__ v, const double* __restrict__ t, Dual* __restrict__ out,
+                            int invd) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int K = blockIdx.z;
+  if (I >= b.nx || J >= b.ny) return;
+  const long long p = (long long)K * b.S + (long long)J * b.P + I;
+  const double x = v[p], y = t[p];
+  out[p] = invd ? Dual(x, -(x * x) * y) : Dual(x, y);
 }
 
-void dual_cycle(const JmgPlan* p, void* ws, void* tws, const CycleParams& cp, int lev, bool fcycle, bool skip_pre,
-                cudaStream_t s) {
-  const Lvl<double> a = lvl64(p, ws, lev), t = lvl64(p, tws, lev);
+// dense (value, tangent) -> pitched Duals; the frame is zeroed (do_BCs) with zero_frame
+__global__ void k_dual_copy_in(Box b, const double* __restrict__ v, const double* __restrict__ t,
+                               Dual* __restrict__ out, int zero_frame) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int K = blockIdx.z;
+  if (I >= b.nx || J >= b.ny) return;
+  const long long q = ((long long)K * b.ny + J) * b.nx + I;
+  Dual x(v[q], t[q]);
+  if (zero_frame) {
+    const bool fr = I < 2 || I >= b.nx - 2 || J < 2 || J >= b.ny - 2 || (b.nz > 1 && (K < 2 || K >= b.nz - 2));
+    if (fr) x = Dual(0.0, 0.0);
+  }
+  out[(long long)K * b.S + (long long)J * b.P + I] = x;
+}
+
+__global__ void k_dual_copy_out(Box b, const Dual* __restrict__ in, double* __restrict__ v, double* __restrict__ t) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int K = blockIdx.z;
+  if (I >= b.nx || J >= b.ny) return;
+  const Dual x = in[(long long)K * b.S + (long long)J * b.P + I];
+  const long long q = ((long long)K * b.ny + J) * b.nx + I;
+  v[q] = x.v;
+  t[q] = x.d;
+}
+
+// distance of the value part (solver_2d.py:481-494: max |phi_old - phi| over the padded
+// box, as ordered bits so that NaN propagates), then phi_old <- phi
+__global__ void k_dual_distance(Box b, double* __restrict__ old_phi, const Dual* __restrict__ phi, LoopState* st) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int K = blockIdx.z;
+  unsigned long long m = 0;
+  if (I < b.nx && J < b.ny) {
+    const long long p = (long long)K * b.S + (long long)J * b.P + I;
+    const double n = phi[p].v;
+    m = abs_bits(old_phi[p] - n);
+    old_phi[p] = n;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, m, o);
+    m = w > m ? w : m;
+  }
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(&st->dist_bits, m);
+}
+
+dim3 box_grid(const Box& b) { return dim3(cdiv(b.nx, 32), cdiv(b.ny, 8), b.nz); }
+
+// multigrid_cycle (solver_2d.py:582-614, solver_3d.py:588-620) over Duals: grid-wide
+// operators above the first coarse level, one single-block launch from there down
+void dual_cycle(const JmgPlan* p, const LvlTable<Dual>& t, const LvlTable<Dual>* dt, const CycleParams& cp, int cs,
+                int lev, bool fcycle, bool skip_pre, cudaStream_t s) {
+  if (lev >= cs) {
+    launch_coarse_cycle<Dual>(p->dim, dt, cp, lev, fcycle ? 1 : 0, skip_pre ? 1 : 0, s);
+    return;
+  }
+  Lvl<Dual> a = t.l[lev];
   if (lev == cp.last_level) {
-    for (int k = 0; k < cp.nu1 + cp.nu2; ++k) dual_sweep(a, t, s);
+    for (int k = 0; k < cp.nu1 + cp.nu2; ++k) launch_sweep<Dual>(p->dim, a, s);
     return;
   }
   if (!skip_pre)
-    for (int k = 0; k < cp.nu1; ++k) dual_sweep(a, t, s);
-  const Lvl<double> ac = lvl64(p, ws, lev + 1), tc = lvl64(p, tws, lev + 1);
-  dim3 b(32, 8), g(cdiv(ac.mx + 3, 32), cdiv(ac.my + 3, 8));
-  k_dual_restrict2d<<<g, b, 0, s>>>(a, t, ac, tc);
+    for (int k = 0; k < cp.nu1; ++k) launch_sweep<Dual>(p->dim, a, s);
+  launch_restrict_grid<Dual>(p->dim, a, t.l[lev + 1], s);
   if (fcycle)
-    for (int k = 0; k < cp.gamma; ++k) dual_cycle(p, ws, tws, cp, lev + 1, true, false, s);
-  for (int k = 0; k < cp.gamma; ++k) dual_cycle(p, ws, tws, cp, lev + 1, false, false, s);
-  launch_prolong<double>(2, a, ac, cp.diag, s);
-  launch_prolong<double>(2, t, tc, cp.diag, s);
-  for (int k = 0; k < cp.nu2; ++k) dual_sweep(a, t, s);
+    for (int g = 0; g < cp.gamma; ++g) dual_cycle(p, t, dt, cp, cs, lev + 1, true, false, s);
+  for (int g = 0; g < cp.gamma; ++g) dual_cycle(p, t, dt, cp, cs, lev + 1, false, false, s);
+  if (p->dim == 2) launch_prolong_cells2d<Dual>(a, t.l[lev + 1], cp.diag, s);
+  else launch_prolong_cells3d<Dual>(a, t.l[lev + 1], cp.diag, s);
+  for (int k = 0; k < cp.nu2; ++k) launch_sweep<Dual>(p->dim, a, s);
+}
+
+bool same_forms(const JmgPlan* p, const JmgCoeffs* c, const JmgCoeffs* d) {
+  if ((c->lam == nullptr) != (d->lam == nullptr)) return false;
+  for (int a = 0; a < p->dim; ++a)
+    if ((c->D[a] == nullptr) != (d->D[a] == nullptr)) return false;
+  return true;
 }
 
 }  // namespace
@@ -137,53 +193,122 @@ using namespace jmg;
 
 extern "C" {
 
-size_t jmg_tangent_workspace_bytes(const JmgPlan* p) { return p ? p->ws_bytes : 0; }
+size_t jmg_tangent_workspace_bytes(const JmgPlan* p) { return p ? tan_layout(p).total : 0; }
+
+int jmg_solve_jvp(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs* c, const double* phi0_dot,
+                  const double* rhs_dot, const JmgCoeffs* c_dot, double* phi_out, double* phi_dot_out,
+                  int64_t* count_out, void* ws, size_t ws_bytes, void* tws, size_t tws_bytes, jmg_stream_t stream) {
+  int rc = check_ws(p, ws, ws_bytes);
+  if (rc) return rc;
+  const TanLayout L = tan_layout(p);
+  if (!tws || tws_bytes < L.total || reinterpret_cast<uintptr_t>(tws) % kAlign != 0)
+    return fail(JMG_ERR_WORKSPACE, "tangent workspace missing, unaligned or smaller than jmg_tangent_workspace_bytes");
+  if (p->mixed || p->fcg)
+    return fail(JMG_ERR_VALUE, "the tangent differentiates the reference's FP64 iteration (precision fp64, outer "
+                               "richardson)");
+  if (!p->cfg.fixed && p->cfg.stop != JMG_STOP_DISTANCE)
+    return fail(JMG_ERR_VALUE, "the tangent follows the reference's loops: fixed=True or the distance stop");
+  if ((rc = check_coeffs(p, c))) return rc;
+  if (!c_dot) return fail(JMG_ERR_VALUE, "coeffs_dot must not be NULL");
+  if ((rc = check_coeffs(p, c_dot))) return rc;
+  if (!same_forms(p, c, c_dot))
+    return fail(JMG_ERR_VALUE, "tangents of lambda and D must be arrays where lambda and D are arrays, scalars "
+                               "where they are scalars");
+  if (!phi0 || !rhs || !phi0_dot || !rhs_dot || !phi_out || !phi_dot_out) return fail(JMG_ERR_VALUE, "NULL argument");
+  if ((rc = coarse_setup(p))) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  const Box b0 = p->lv[0].box;
+  // coefficients and their tangents: the plan's hierarchy of c in ws and of c_dot in tws,
+  // packed into Duals ((1/A_cc)' = -(1/A_cc)^2 A_cc')
+  if ((rc = build_hierarchy(p, c, ws, s))) return rc;
+  if ((rc = build_hierarchy(p, c_dot, tws, s))) return rc;
+  LvlTable<Dual> tab;
+  memset(&tab, 0, sizeof(tab));
+  for (int l = 0; l < p->used; ++l) {
+    const Lvl<double> a = lvl64(p, ws, l), t = lvl64(p, tws, l);
+    const Lvl<Dual> d = dual_lvl(p, tws, L, l);
+    const Box& b = p->lv[l].box;
+    const dim3 g = box_grid(b), blk(32, 8, 1);
+    k_pack_dual<<<g, blk, 0, s>>>(b, a.wx, t.wx, d.wx, 0);
+    k_pack_dual<<<g, blk, 0, s>>>(b, a.wy, t.wy, d.wy, 0);
+    if (p->dim == 3) k_pack_dual<<<g, blk, 0, s>>>(b, a.wz, t.wz, d.wz, 0);
+    k_pack_dual<<<g, blk, 0, s>>>(b, a.acc, t.acc, d.acc, 0);
+    k_pack_dual<<<g, blk, 0, s>>>(b, a.invd, t.acc, d.invd, 1);
+    if (p->off_diag) {
+      k_pack_dual<<<g, blk, 0, s>>>(b, a.xll, t.xll, d.xll, 0);
+      k_pack_dual<<<g, blk, 0, s>>>(b, a.xrl, t.xrl, d.xrl, 0);
+      k_pack_dual<<<g, blk, 0, s>>>(b, a.xlr, t.xlr, d.xlr, 0);
+      k_pack_dual<<<g, blk, 0, s>>>(b, a.xrr, t.xrr, d.xrr, 0);
+    }
+    tab.l[l] = d;
+  }
+  LvlTable<Dual>* dtab = ptr<LvlTable<Dual>>(tws, L.tab);
+  launch_store_table<Dual>(tab, dtab, s);
+  // inputs; phi_old keeps phi0 with its frame (the first distance sees it, solver_2d.py:471)
+  Lvl<Dual> d0 = tab.l[0];
+  double* phi_old = ptr<double>(tws, L.phi_old);
+  LoopState* st = ptr<LoopState>(tws, L.state);
+  k_dual_copy_in<<<box_grid(b0), dim3(32, 8, 1), 0, s>>>(b0, phi0, phi0_dot, d0.phi, 1);
+  k_dual_copy_in<<<box_grid(b0), dim3(32, 8, 1), 0, s>>>(b0, rhs, rhs_dot, d0.rhs, 1);
+  launch_copy_in(b0, phi0, phi_old, 0, s);
+  const CycleParams cp = cycle_params(p, p->off_diag);
+  // the coarse kernel of the solve: the single block from the same level as jmg_solve's
+  const int cs = p->cluster_ranks ? block_coarse_level(p) : p->coarse_start;
+  const int mode = p->cfg.fixed ? 2 : 0;
+  // skip_pre: pre-smoothing once, before the loop (solver_2d.py:457-459)
+  const bool presmoothed = p->cfg.skip_pre && cp.nu1 > 0;
+  if (presmoothed) {
+    for (int k = 0; k < cp.nu1; ++k) launch_sweep<Dual>(p->dim, d0, s);
+    k_dual_distance<<<box_grid(b0), dim3(32, 8, 1), 0, s>>>(b0, phi_old, d0.phi, st);  // phi_old <- smoothed phi
+  }
+  const bool runs = p->cfg.max_iters_outer > 0;
+  if (runs) {
+    launch_loop_init(st, nullptr, 0, mode, p->cfg.rtol, p->cfg.max_iters_outer, 0, s);
+    if (mode == 2) {
+      for (long long it = 0; it < p->cfg.max_iters_outer; ++it)
+        dual_cycle(p, tab, dtab, cp, cs, 0, p->cfg.fcycle != 0, p->cfg.skip_pre != 0, s);
+    } else {
+      for (;;) {
+        int go = 0;
+        cudaError_t e = cudaMemcpyAsync(&go, &st->go, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return fail(JMG_ERR_CUDA, cudaGetErrorString(e));
+        if (!go) break;
+        dual_cycle(p, tab, dtab, cp, cs, 0, p->cfg.fcycle != 0, p->cfg.skip_pre != 0, s);
+        k_dual_distance<<<box_grid(b0), dim3(32, 8, 1), 0, s>>>(b0, phi_old, d0.phi, st);
+        launch_loop_step(st, nullptr, 0, mode, p->cfg.epsilon, p->cfg.rtol, p->cfg.max_iters_outer, 0, s);
+      }
+    }
+  }
+  // outputs; with no cycle and no smoothing phi0 and its tangent come back untouched
+  const size_t dense = (size_t)b0.nx * b0.ny * b0.nz * 8;
+  if (runs || presmoothed) {
+    k_dual_copy_out<<<box_grid(b0), dim3(32, 8, 1), 0, s>>>(b0, d0.phi, phi_out, phi_dot_out);
+  } else {
+    if (phi_out != phi0) cudaMemcpyAsync(phi_out, phi0, dense, cudaMemcpyDeviceToDevice, s);
+    if (phi_dot_out != phi0_dot) cudaMemcpyAsync(phi_dot_out, phi0_dot, dense, cudaMemcpyDeviceToDevice, s);
+  }
+  if (count_out) {
+    if (mode == 2 || !runs) {
+      const long long n = runs ? p->cfg.max_iters_outer : 0;
+      cudaMemcpyAsync(count_out, &n, sizeof(n), cudaMemcpyHostToDevice, s);
+      cudaStreamSynchronize(s);  // n lives on this stack frame
+    } else {
+      launch_count_out(st, (long long*)count_out, s);
+    }
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(JMG_ERR_CUDA, cudaGetErrorString(e));
+  return JMG_OK;
+}
 
 int jmg_solve_fixed_jvp(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs* c,
                         const double* phi0_dot, const double* rhs_dot, const JmgCoeffs* c_dot, double* phi_out,
                         double* phi_dot_out, void* ws, size_t ws_bytes, void* tws, size_t tws_bytes,
                         jmg_stream_t stream) {
-  int rc = check_ws(p, ws, ws_bytes);
-  if (rc) return rc;
-  if ((rc = check_ws(p, tws, tws_bytes))) return rc;
-  if (p->dim != 2) return fail(JMG_ERR_VALUE, "the tangent is implemented for 2D solves");
-  if (!p->cfg.fixed) return fail(JMG_ERR_VALUE, "the tangent follows the fixed mode (fixed=True)");
-  if (p->mixed || p->fcg || p->off_diag)
-    return fail(JMG_ERR_VALUE, "the tangent differentiates the FP64 5-point iteration of the reference");
-  if ((rc = check_coeffs(p, c))) return rc;
-  if (!c_dot || !phi0 || !rhs || !phi0_dot || !rhs_dot || !phi_out || !phi_dot_out)
-    return fail(JMG_ERR_VALUE, "NULL argument");
-  for (int a = 0; a < 2; ++a)
-    if ((c->D[a] == nullptr) != (c_dot->D[a] == nullptr))
-      return fail(JMG_ERR_VALUE, "tangent D components must be arrays where D is, scalars where it is");
-  if ((c->lam == nullptr) != (c_dot->lam == nullptr))
-    return fail(JMG_ERR_VALUE, "the tangent of lambda must be an array where lambda is, a scalar where it is");
-  cudaStream_t s = (cudaStream_t)stream;
-  const Box b0 = p->lv[0].box;
-  Lvl<double> a0 = lvl64(p, ws, 0), t0 = lvl64(p, tws, 0);
-  // inputs; the frame of phi is zero at every cycle in fixed mode (solver_2d.py:462)
-  launch_copy_in(b0, phi0, a0.phi, 1, s);
-  launch_copy_in(b0, rhs, a0.rhs, 1, s);
-  launch_copy_in(b0, phi0_dot, t0.phi, 1, s);
-  launch_copy_in(b0, rhs_dot, t0.rhs, 1, s);
-  // coefficients and their tangents (linear hierarchy; then d(1/A_cc))
-  if ((rc = build_hierarchy(p, c, ws, s))) return rc;
-  if ((rc = build_hierarchy(p, c_dot, tws, s))) return rc;
-  for (int l = 0; l < p->used; ++l) {
-    const Lvl<double> a = lvl64(p, ws, l), t = lvl64(p, tws, l);
-    dim3 b(32, 8), g(cdiv(a.mx + 3, 32), cdiv(a.my + 3, 8));
-    k_tan_invd<<<g, b, 0, s>>>(a, t);
-  }
-  const CycleParams cp = cycle_params(p, false);
-  if (p->cfg.skip_pre)
-    for (int k = 0; k < cp.nu1; ++k) dual_sweep(a0, t0, s);
-  for (long long it = 0; it < p->cfg.max_iters_outer; ++it)
-    dual_cycle(p, ws, tws, cp, 0, p->cfg.fcycle != 0, p->cfg.skip_pre != 0, s);
-  launch_copy_out(b0, a0.phi, phi_out, s);
-  launch_copy_out(b0, t0.phi, phi_dot_out, s);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return fail(JMG_ERR_CUDA, cudaGetErrorString(e));
-  return JMG_OK;
+  if (p && !p->cfg.fixed) return fail(JMG_ERR_VALUE, "jmg_solve_fixed_jvp needs a plan with fixed = 1");
+  return jmg_solve_jvp(p, phi0, rhs, c, phi0_dot, rhs_dot, c_dot, phi_out, phi_dot_out, nullptr, ws, ws_bytes, tws,
+                       tws_bytes, stream);
 }
 
 }  // extern "C"

@@ -2,6 +2,7 @@
 // the defect + restriction onto the next level and the FP64 residual of a refinement step.
 #include "mg_common.cuh"
 #include "mg_kernels.h"
+#include "mg_dual.cuh"
 
 namespace jmg {
 
@@ -207,6 +208,8 @@ void launch_prolong_cells2d(const Lvl<T>& f, const Lvl<T>& c, int diag, cudaStre
 
 template void launch_prolong_cells2d<double>(const Lvl<double>&, const Lvl<double>&, int, cudaStream_t);
 template void launch_prolong_cells2d<float>(const Lvl<float>&, const Lvl<float>&, int, cudaStream_t);
+// the forward-mode solve (mg_tangent.cu)
+template void launch_prolong_cells2d<Dual>(const Lvl<Dual>&, const Lvl<Dual>&, int, cudaStream_t);
 
 template void launch_restrict_tile2d<double>(const Lvl<double>&, const Lvl<double>&, cudaStream_t);
 template void launch_restrict_tile2d<float>(const Lvl<float>&, const Lvl<float>&, cudaStream_t);

@@ -13,6 +13,7 @@
 // k_restrict3d. Also phi_c = 0 on the whole padded coarse box.
 #include "mg_common.cuh"
 #include "mg_kernels.h"
+#include "mg_dual.cuh"
 
 namespace jmg {
 
@@ -190,6 +191,8 @@ void launch_prolong_cells3d(const Lvl<T>& f, const Lvl<T>& c, int bilinear, cuda
 
 template void launch_prolong_cells3d<double>(const Lvl<double>&, const Lvl<double>&, int, cudaStream_t);
 template void launch_prolong_cells3d<float>(const Lvl<float>&, const Lvl<float>&, int, cudaStream_t);
+// the forward-mode solve (mg_tangent.cu)
+template void launch_prolong_cells3d<Dual>(const Lvl<Dual>&, const Lvl<Dual>&, int, cudaStream_t);
 template void launch_restrict_tile3d<double>(const Lvl<double>&, const Lvl<double>&, cudaStream_t);
 template void launch_restrict_tile3d<float>(const Lvl<float>&, const Lvl<float>&, cudaStream_t);
 
