@@ -38,9 +38,11 @@ struct Lvl {
   int mx, my, mz;  // resolution per axis (interior indices 2..m)
   int P;           // row pitch in elements
   long long S;     // plane stride in elements (3D)
-  // second phi buffer of a level swept in one pass (launch_sweep_fused3d writes it and
-  // swaps the two); nullptr where the level uses the in-place colour passes
+  // second phi buffer of a level swept in one pass or by the fused operator pairs (those
+  // kernels write it and swap the two); nullptr where the level uses in-place passes only
   T* phi2;
+  int onepass;  // the level's sweeps run in one pass (needs phi2)
+  int fuseops;  // 2D: smooth + restrict and prolong + smooth as fused tile kernels (needs phi2)
 };
 
 constexpr int kMaxLevels = 16;

@@ -53,12 +53,17 @@ int set_err(int code, const char* fmt, ...) {
 // of 256 to 8192 points measured on GB300: 2048 is fastest for the 2D and 3D solves in
 // FP64 and in mixed precision; at 8192 the block spends longer on the 64^2 / 16^3 level
 // than one grid-wide launch per operator takes.
-int block_coarse_start(const JmgPlan* p) {
+long long coarse_block_points() {
   static const long long limit = [] {
     const char* e = getenv("JMG_COARSE_POINTS");  // tuning knob; 2048 by default
     const long long v = e ? atoll(e) : 0;
     return v > 0 ? v : 2048LL;
   }();
+  return limit;
+}
+
+int block_coarse_start(const JmgPlan* p) {
+  const long long limit = coarse_block_points();
   for (int l = 0; l < p->used; ++l) {
     const long long pts = (long long)p->lv[l].box.nx * p->lv[l].box.ny * p->lv[l].box.nz;
     if (pts <= limit) return l;
@@ -128,6 +133,22 @@ int validate_and_layout(JmgPlan* p) {
   const bool fused64 = fused_on && fe64 && fe64[0] == '1';
   const char* fe2 = getenv("JMG_FUSED2D");
   const bool fused2d = fe2 && fe2[0] == '1';
+  // fused operator pairs (mg_fusedops2d.cu) on the 2D levels the grid-wide kernels run
+  // (more points than the single-block coarse kernel takes), 5-point stencil;
+  // JMG_FUSEDOPS=0 turns them off
+  const char* fo = getenv("JMG_FUSEDOPS");
+  const bool fuseops_on = d == 2 && !p->off_diag && !(fo && fo[0] == '0');
+  const long long block_limit = coarse_block_points();
+  // Largest fused level (padded points): every FP32 level, FP64 levels up to 2^19 points.
+  // On larger FP64 levels the halos' extra FP64 work outweighs the saved launches (2D
+  // 1024^2 plain FP64, measured: 40.7 ms with the 512^2 level and below fused, 43.5 ms
+  // with level 0 too, 42.0 ms unfused; mixed + FCG 6.97 ms all fused, 7.73 ms unfused).
+  // JMG_FUSEDOPS_MAX overrides it.
+  const long long fuse_max = [&] {
+    const char* e = getenv("JMG_FUSEDOPS_MAX");
+    const long long v = e ? atoll(e) : 0;
+    return v > 0 ? v : (p->mixed ? (1LL << 62) : (1LL << 19));
+  }();
   size_t off = 0;
   auto take = [&](size_t bytes) {
     const size_t o = off;
@@ -160,10 +181,14 @@ int validate_and_layout(JmgPlan* p) {
         (fused_min > 0 ? (long long)li.elems >= fused_min
                        : d == 3 ? fused_wave_permille(li.m[0], li.m[1], li.m[2]) >= 500
                                 : fused2d && (long long)li.elems >= (1LL << 18));
-    li.phi2 = fused_level && fused64 ? take(b8) : 0;
+    li.onepass64 = fused_level && fused64;
+    li.onepass32 = fused_level && p->mixed;
+    const long long pts = (long long)li.box.nx * li.box.ny * li.box.nz;
+    li.fuse_ops = fuseops_on && l + 1 < p->used && pts > block_limit && pts <= fuse_max;
+    li.phi2 = li.onepass64 || (li.fuse_ops && !p->mixed) ? take(b8) : 0;
     li.phi2_32 = 0;
     if (p->mixed) {
-      if (fused_level) li.phi2_32 = take(b4);
+      if (li.onepass32 || li.fuse_ops) li.phi2_32 = take(b4);
       li.phi32 = take(b4);
       li.rhs32 = take(b4);
       li.wx32 = take(b4);
@@ -267,6 +292,7 @@ int jmg::coarse_setup(JmgPlan* p) {
     const size_t b = coarse_smem32_bytes(mx, my, p->coarse_start, last);
     if (b <= 200 * 1024 && prepare_coarse_smem32(b) == 0) p->coarse_smem32 = b;
   }
+  prepare_fused_ops2d();  // kernel attributes, set outside any stream capture
   cudaGetLastError();  // a refused attribute or occupancy query leaves no sticky error
   p->coarse_ready = true;
   return JMG_OK;
@@ -289,6 +315,8 @@ Lvl<double> jmg::lvl64(const JmgPlan* p, void* ws, int l) {
   a.invd = ptr<double>(ws, li.invd);
   a.acc = ptr<double>(ws, li.acc);
   a.phi2 = li.phi2 ? ptr<double>(ws, li.phi2) : nullptr;
+  a.onepass = li.onepass64 ? 1 : 0;
+  a.fuseops = li.fuse_ops && li.phi2 ? 1 : 0;
   a.mx = li.m[0];
   a.my = li.m[1];
   a.mz = li.m[2];
@@ -316,6 +344,8 @@ Lvl<float> jmg::lvl32(const JmgPlan* p, void* ws, int l) {
   a.invd = ptr<float>(ws, li.invd32);
   a.acc = ptr<float>(ws, li.acc32);
   a.phi2 = li.phi2_32 ? ptr<float>(ws, li.phi2_32) : nullptr;
+  a.onepass = li.onepass32 ? 1 : 0;
+  a.fuseops = li.fuse_ops && li.phi2_32 ? 1 : 0;
   a.mx = li.m[0];
   a.my = li.m[1];
   a.mz = li.m[2];
@@ -366,16 +396,24 @@ struct EmitTop {
 
 // multigrid_cycle, solver_2d.py:582-614, emitted as launches on stream s. With a
 // non-null `count`, nothing is launched and the number of kernel launches is added.
+// zero_phi: phi of this level is zero on entry (the first visit after the restriction
+// above zeroed it), so a fused pre-sweep need not read it.
 template <typename T>
 void emit_cycle(const JmgPlan* p, LvlTable<T>& tab, const LvlTable<T>* dtab, const CycleParams& cp, int lev,
                 bool fcycle, bool skip_pre, cudaStream_t s, long long* count = nullptr,
-                const EmitTop* top = nullptr) {
+                const EmitTop* top = nullptr, bool zero_phi = false) {
   const int dim = p->dim;
+  // Fused operator pairs on a grid-wide 2D level (mg_fusedops2d.cu): the last pre-sweep
+  // with the restriction, the prolongation with the first post-sweep; each writes the
+  // level's second buffer and swaps, so a visit swaps twice.
+  const bool fuse = lev < p->coarse_start && lev != cp.last_level && tab.l[lev].fuseops && !tab.l[lev].xll &&
+                    !skip_pre && cp.nu1 >= 1 && cp.nu2 >= 1;
   // One-pass sweeps write the level's second buffer and swap; an even number of them per
   // visit leaves phi where the visit found it (the restriction, the prolongation and the
   // caller's tables see the current buffer). An odd remainder runs as colour passes.
-  const int nsweeps = lev == cp.last_level ? cp.nu1 + cp.nu2 : (skip_pre ? 0 : cp.nu1) + cp.nu2;
-  int fused_left = tab.l[lev].phi2 ? nsweeps - nsweeps % 2 : 0;
+  const int nsweeps = lev == cp.last_level ? cp.nu1 + cp.nu2
+                                           : (skip_pre ? 0 : cp.nu1) + cp.nu2 - (fuse ? 2 : 0);
+  int fused_left = tab.l[lev].onepass ? nsweeps - nsweeps % 2 : 0;
   auto sweep = [&](bool first) {
     const bool zero = top && top->zero_first && first;
     if (fused_left > 0) {
@@ -403,15 +441,26 @@ void emit_cycle(const JmgPlan* p, LvlTable<T>& tab, const LvlTable<T>* dtab, con
     return;
   }
   if (!skip_pre)
-    for (int k = 0; k < cp.nu1; ++k) sweep(k == 0);
+    for (int k = 0; k < cp.nu1 - (fuse ? 1 : 0); ++k) sweep(k == 0);
   if (count) *count += 1;
+  else if (fuse)
+    launch_smooth_restrict2d<T>(tab.l[lev], tab.l[lev + 1],
+                                cp.nu1 == 1 && ((top && top->zero_first) || zero_phi), s);
   else launch_restrict<T>(dim, tab.l[lev], tab.l[lev + 1], s);
+  bool first = true;  // phi of level lev + 1 is zero until its first visit
   if (fcycle)
-    for (int g = 0; g < cp.gamma; ++g) emit_cycle<T>(p, tab, dtab, cp, lev + 1, true, false, s, count);
-  for (int g = 0; g < cp.gamma; ++g) emit_cycle<T>(p, tab, dtab, cp, lev + 1, false, false, s, count);
+    for (int g = 0; g < cp.gamma; ++g) {
+      emit_cycle<T>(p, tab, dtab, cp, lev + 1, true, false, s, count, nullptr, first);
+      first = false;
+    }
+  for (int g = 0; g < cp.gamma; ++g) {
+    emit_cycle<T>(p, tab, dtab, cp, lev + 1, false, false, s, count, nullptr, first);
+    first = false;
+  }
   if (count) *count += 1;
+  else if (fuse) launch_prolong_smooth2d<T>(tab.l[lev], tab.l[lev + 1], s);
   else launch_prolong<T>(dim, tab.l[lev], tab.l[lev + 1], cp.diag, s);
-  for (int k = 0; k < cp.nu2; ++k) sweep(false);
+  for (int k = 0; k < cp.nu2 - (fuse ? 1 : 0); ++k) sweep(false);
 }
 
 // Whether the mixed-precision refinement step can use the short form: the FP32 cycle
@@ -750,7 +799,7 @@ bool jmg::pdl_enabled() {
 // level has a second buffer (phi ends in the buffer it started in), colour passes else
 template <typename T>
 static void smooth_like_solve(const JmgPlan* p, Lvl<T>& a, int nsweeps, cudaStream_t s) {
-  const int fused = a.phi2 ? nsweeps - nsweeps % 2 : 0;
+  const int fused = a.onepass ? nsweeps - nsweeps % 2 : 0;
   for (int k = 0; k < fused; ++k) launch_sweep_onepass<T>(p->dim, a, false, s);
   for (int k = fused; k < nsweeps; ++k) launch_sweep<T>(p->dim, a, s);
 }
@@ -1098,7 +1147,7 @@ int jmg_plan_coarse_start(const JmgPlan* p) { return p ? p->coarse_start : -1; }
 int jmg_plan_sweep_launches(const JmgPlan* p, int level, int fp32) {
   if (!p || level < 0 || level >= p->used) return 0;
   const LevelInfo& li = p->lv[level];
-  if (fp32 ? li.phi2_32 != 0 : li.phi2 != 0) return 1;
+  if (fp32 ? li.onepass32 : li.onepass64) return 1;
   return p->off_diag ? 4 : 2;
 }
 

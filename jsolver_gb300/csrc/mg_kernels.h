@@ -57,6 +57,13 @@ template <typename T> void launch_prolong_cells2d(const Lvl<T>& f, const Lvl<T>&
 int fused_chunk3d(int mx, int my, int mz, int blocks_per_sm);
 int fused_blocks3d(int mx, int my, int mz);
 int fused_wave_permille(int mx, int my, int mz);
+// mg_fusedops2d.cu: 2D operator pairs over tiles with halos; each writes f.phi2 and swaps
+// f.phi / f.phi2. smooth_restrict: the last pre-sweep, then defect + restriction onto c
+// (and phi_c = 0); zero_in: f.phi is zero (not read). prolong_smooth: phi += P phi_c, then
+// one sweep (levels with nu2 >= 1 and no D_xy).
+template <typename T> void launch_smooth_restrict2d(Lvl<T>& f, const Lvl<T>& c, bool zero_in, cudaStream_t s);
+template <typename T> void launch_prolong_smooth2d(Lvl<T>& f, const Lvl<T>& c, cudaStream_t s);
+void prepare_fused_ops2d();
 // mg_tile2d.cu: defect + restriction with every fine defect computed once
 template <typename T> void launch_restrict_tile2d(const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s);
 // mg_tile2d.cu: r32 = float(rhs - L_h phi) (FP64 arithmetic) on the interior, and per-block

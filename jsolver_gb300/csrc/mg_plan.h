@@ -20,7 +20,10 @@ struct LevelInfo {
   size_t d[3];                              // 3D averaged D (levels >= 1)
   size_t phi32, rhs32, wx32, wy32, wz32, invd32, acc32;  // FP32 mirrors (mixed precision)
   size_t xd[4], xd32[4];  // 2D with D_xy: A_ll, A_rl, A_lr, A_rr (FP64, FP32 mirrors); 0 if absent
-  size_t phi2, phi2_32;   // second phi buffers of one-pass swept levels (FP64, FP32); 0 if absent
+  size_t phi2, phi2_32;   // second phi buffers (FP64, FP32) of levels swept in one pass or by
+                          // the fused operator pairs; 0 if absent
+  bool onepass64, onepass32;  // sweeps in one pass (FP64, FP32 arrays)
+  bool fuse_ops;              // 2D grid-wide level: fused smooth + restrict, prolong + smooth
 };
 
 }  // namespace jmg

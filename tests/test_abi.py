@@ -74,6 +74,7 @@ def test_config_extensions_are_validated_without_gpu():
 
 def test_launch_counts_follow_the_form(monkeypatch):
     monkeypatch.setenv("JMG_FUSED", "0")  # the same sweeps in both forms
+    monkeypatch.setenv("JMG_FUSEDOPS", "0")  # and the same operators
     lib = _lib.load()
     g = _engine.make_grid((grid_1D(1024), grid_1D(1024)))
     counts = {}
@@ -85,6 +86,31 @@ def test_launch_counts_follow_the_form(monkeypatch):
         counts[name] = b.value
     # an FCG step adds its four vector kernels to the cycle and the stopping test
     assert counts["fcg"] >= counts["plain"] + 3
+
+
+def test_fused_operator_pairs_cut_launches(monkeypatch):
+    """2D grid-wide levels run smooth + restrict and prolong + smooth as two fused
+    launches per visit instead of six (two colour passes per sweep, restriction,
+    prolongation): every FP32 level, FP64 levels up to 2^19 padded points."""
+    lib = _lib.load()
+    g = _engine.make_grid((grid_1D(1024), grid_1D(1024)))
+
+    def per_cycle(env, **kw):
+        monkeypatch.delenv("JMG_FUSEDOPS", raising=False)
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        p = _lib.Plan(g, _engine.make_config(**kw))
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        assert lib.jmg_plan_launch_counts(p.handle, ctypes.byref(a), ctypes.byref(b)) == 0
+        return b.value
+
+    # V(1,1) over 11 levels: levels 0 .. 4 grid-wide (6 launches each unfused, 2 fused)
+    fp32_off = per_cycle({"JMG_FUSEDOPS": "0"}, stop="residual", precision="mixed", outer="fcg", inner_cycles=1)
+    fp32_on = per_cycle({}, stop="residual", precision="mixed", outer="fcg", inner_cycles=1)
+    assert fp32_off - fp32_on == 5 * 4
+    fp64_off = per_cycle({"JMG_FUSEDOPS": "0"})
+    fp64_on = per_cycle({})
+    assert fp64_off - fp64_on == 4 * 4  # level 0 (1027^2 points) is not fused in FP64
 
 
 def test_sweep_launches_per_level(monkeypatch):

@@ -151,3 +151,51 @@ def test_cell_prolongation_2d_equals_grid(monkeypatch, shape, opts):
     got, c_got = run({})
     assert int(c_got) == int(c_ref)
     assert torch.equal(got, ref)
+
+
+CASES_OPS = [
+    ((256, 256), dict(precision="mixed", stop="residual", outer="fcg", inner_cycles=2)),
+    ((1024, 1024), dict(precision="mixed", stop="residual", outer="fcg", inner_cycles=2)),
+    ((256, 256), dict(precision="mixed", stop="residual")),
+    ((512, 512), dict(stop="residual", outer="fcg")),
+    ((128, 256), dict(precision="mixed", fixed=True, max_iters_outer=6, gamma=2)),
+    ((256, 128), dict(fixed=True, max_iters_outer=5, nu1=2, nu2=1)),
+    ((256, 256), dict(fixed=True, max_iters_outer=5, nu1=1, nu2=2)),
+    ((256, 256), dict(fixed=True, max_iters_outer=4, nu1=0, nu2=2)),
+    ((256, 256), dict(fixed=True, max_iters_outer=4, nu1=2, nu2=0)),
+    ((256, 256), dict(fixed=True, max_iters_outer=5, skip_pre=True, fcycle=True)),
+    ((256, 256), dict(fixed=True, max_iters_outer=4, fcycle=True, gamma=2)),
+    ((64, 256), dict(fixed=True, max_iters_outer=3)),
+    ((256, 256), dict()),
+]
+
+
+@pytest.mark.parametrize("shape,opts", CASES_OPS, ids=lambda x: str(x))
+def test_fused_operator_pairs_2d_equal_unfused(monkeypatch, shape, opts):
+    """2D solves with the fused pairs (smooth + restrict, prolong + smooth over tiles with
+    halos; the default on grid-wide 2D levels) and with the separate colour passes,
+    tiled restriction and cell prolongation (JMG_FUSEDOPS=0): the same bits and counts,
+    in FP64 and FP32 cycles, every cycle shape and sweep count, FCG and Richardson."""
+    from jsolver_gb300 import workloads as W
+    from jsolver_gb300.solver_2d import solve_2d
+    mx, my = shape
+    p = W.random_2d(max(mx, my), seed=5 * mx + my)
+    sl = (slice(0, my + 3), slice(0, mx + 3))
+    args = [torch.from_numpy(np.ascontiguousarray(p[k][sl])).to(DEV) for k in ("phi0", "rhs", "lam", "D_xx", "D_yy")]
+    args[1] = args[1].clone()
+    args[1][-2:, :] = 0  # the frame where the slice cut the field
+    args[1][:, -2:] = 0
+    grids = (grid_1D(mx), grid_1D(my))
+
+    def run(env):
+        monkeypatch.delenv("JMG_FUSEDOPS", raising=False)
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        _engine.CACHE.plans.clear()
+        _engine.CACHE.ws.clear()
+        return solve_2d(*grids, *args, **opts)
+
+    ref, c_ref = run({"JMG_FUSEDOPS": "0"})
+    got, c_got = run({})
+    assert int(c_got) == int(c_ref)
+    assert torch.equal(got, ref)
