@@ -1,11 +1,14 @@
 // mg_block.cuh — the multigrid operators run by one thread block over a whole level,
-// with a block barrier after each pass: the single-block coarse cycle (k_coarse_cycle)
-// and the single-block coarse segments of the adjoint (mg_adjoint_kernels.cu) use them.
+// with a block barrier after each pass, and the coarse recursion over them: the
+// single-block coarse cycles (k_coarse_cycle over global memory, k_coarse_staged over
+// shared memory) and the single-block coarse segments of the adjoint
+// (mg_adjoint_kernels.cu) use them.
 // Each pass evaluates the same per-point functions (mg_common.cuh) as the grid-wide
 // kernels, so a level gives the same bits whichever runs it.
 #pragma once
 
 #include "mg_common.cuh"
+#include "mg_kernels.h"
 
 namespace jmg {
 
@@ -90,6 +93,58 @@ __device__ void blk_prolong(const Lvl<T>& f, const Lvl<T>& c, bool diag) {
     else prolong_cell3d<T>(f, c, K, J, I, diag);
   }
   __syncthreads();
+}
+
+// multigrid_cycle (solver_2d.py:582-614) restricted to levels >= lev, run by one block.
+// The recursion is unrolled into an explicit stack of frames (no device recursion, so the
+// per-thread stack stays within its default size). Every thread walks the same frames,
+// so the __syncthreads inside the operators are reached uniformly.
+template <typename T, int DIM>
+__device__ void blk_cycle(const LvlTable<T>* __restrict__ tab, const CycleParams& cp, int lev0, bool fcycle0,
+                          bool skip_pre0) {
+  struct Frame {
+    int lev, stage, g;
+    bool fcycle, skip_pre;
+  };
+  Frame st[kMaxLevels + 1];
+  int sp = 0;
+  st[sp++] = Frame{lev0, 0, 0, fcycle0, skip_pre0};
+  while (sp > 0) {
+    Frame& f = st[sp - 1];
+    const Lvl<T> a = tab->l[f.lev];
+    if (f.lev == cp.last_level) {
+      for (int s = 0; s < cp.nu1 + cp.nu2; ++s) blk_sweep<T, DIM>(a);
+      --sp;
+      continue;
+    }
+    if (f.stage == 0) {
+      if (!f.skip_pre)
+        for (int s = 0; s < cp.nu1; ++s) blk_sweep<T, DIM>(a);
+      blk_restrict<T, DIM>(a, tab->l[f.lev + 1]);
+      f.stage = f.fcycle ? 1 : 2;
+      f.g = 0;
+    }
+    if (f.stage == 1) {  // F-cycle: gamma recursive F-cycles first (solver_2d.py:609-610)
+      if (f.g < cp.gamma) {
+        ++f.g;
+        st[sp++] = Frame{f.lev + 1, 0, 0, true, false};
+        continue;
+      }
+      f.stage = 2;
+      f.g = 0;
+    }
+    if (f.stage == 2) {  // gamma plain cycles (solver_2d.py:611)
+      if (f.g < cp.gamma) {
+        ++f.g;
+        st[sp++] = Frame{f.lev + 1, 0, 0, false, false};
+        continue;
+      }
+      f.stage = 3;
+    }
+    blk_prolong<T, DIM>(a, tab->l[f.lev + 1], cp.diag != 0);
+    for (int s = 0; s < cp.nu2; ++s) blk_sweep<T, DIM>(a);
+    --sp;
+  }
 }
 
 }  // namespace jmg

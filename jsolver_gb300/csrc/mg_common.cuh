@@ -63,6 +63,9 @@ __device__ __forceinline__ void pdl_enter() {
 template <typename T>
 struct LvlTable {
   Lvl<T> l[kMaxLevels];
+  // set to 1 by a coarse kernel whose wait for its staging copies ran out (the table is
+  // stored afresh, with 0, at every solve)
+  int fault;
 };
 
 // Red (first) colour of a full sweep. In 2D the reference's first two sub-lattices

@@ -279,6 +279,23 @@ int jmg::coarse_setup(JmgPlan* p) {
       break;
     }
   }
+  // The single block stages its levels in shared memory unless JMG_COARSE=global asks for
+  // the global-memory kernel; JMG_COARSE_THREADS sets its block size (512 by default).
+  p->coarse_staged64 = p->coarse_staged32 = 0;
+  {
+    const char* cg = getenv("JMG_COARSE");
+    const char* ct = getenv("JMG_COARSE_THREADS");
+    const int nt = ct ? atoi(ct) : 0;
+    p->coarse_threads = (nt >= 64 && nt <= 512 && nt % 32 == 0) ? nt : 512;
+    if (!p->cluster_ranks && !(cg && std::strcmp(cg, "global") == 0) && p->used <= kMaxLevels) {
+      size_t elems[kMaxLevels];
+      for (int l = 0; l < p->used; ++l) elems[l] = p->lv[l].elems;
+      const size_t b64 = coarse_staged_bytes(dim, elems, p->coarse_start, last, 8, p->off_diag);
+      if (b64 && prepare_coarse_staged<double>(dim, b64) == 0) p->coarse_staged64 = b64;
+      const size_t b32 = coarse_staged_bytes(dim, elems, p->coarse_start, last, 4, p->off_diag);
+      if (p->mixed && b32 && prepare_coarse_staged<float>(dim, b32) == 0) p->coarse_staged32 = b32;
+    }
+  }
   p->coarse_smem32 = 0;
   const char* c32 = getenv("JMG_COARSE32");
   // opt-in (JMG_COARSE32=smem): staging ~150 KB per launch costs more than the L2 round
@@ -433,6 +450,9 @@ void emit_cycle(const JmgPlan* p, LvlTable<T>& tab, const LvlTable<T>* dtab, con
     else if (sizeof(T) == 4 && p->coarse_smem32)
       launch_coarse_smem32(reinterpret_cast<const LvlTable<float>*>(dtab), cp, lev, fcycle ? 1 : 0,
                            skip_pre ? 1 : 0, p->coarse_smem32, s);
+    else if (lev == p->coarse_start && (sizeof(T) == 8 ? p->coarse_staged64 : p->coarse_staged32))
+      launch_coarse_staged<T>(dim, dtab, cp, lev, fcycle ? 1 : 0, skip_pre ? 1 : 0,
+                              sizeof(T) == 8 ? p->coarse_staged64 : p->coarse_staged32, p->coarse_threads, s);
     else launch_coarse_cycle<T>(dim, dtab, cp, lev, fcycle ? 1 : 0, skip_pre ? 1 : 0, s);
     return;
   }

@@ -117,58 +117,6 @@ __global__ void k_prolong3d(Lvl<T> f, Lvl<T> c, int bilinear) {
 // single-block coarse cycle
 // ------------------------------------------------------------------------------------
 
-// multigrid_cycle (solver_2d.py:582-614) restricted to levels >= lev, run by one block.
-// The recursion is unrolled into an explicit stack of frames (no device recursion, so the
-// per-thread stack stays within its default size). Every thread walks the same frames,
-// so the __syncthreads inside the operators are reached uniformly.
-template <typename T, int DIM>
-__device__ void blk_cycle(const LvlTable<T>* __restrict__ tab, const CycleParams& cp, int lev0, bool fcycle0,
-                          bool skip_pre0) {
-  struct Frame {
-    int lev, stage, g;
-    bool fcycle, skip_pre;
-  };
-  Frame st[kMaxLevels + 1];
-  int sp = 0;
-  st[sp++] = Frame{lev0, 0, 0, fcycle0, skip_pre0};
-  while (sp > 0) {
-    Frame& f = st[sp - 1];
-    const Lvl<T> a = tab->l[f.lev];
-    if (f.lev == cp.last_level) {
-      for (int s = 0; s < cp.nu1 + cp.nu2; ++s) blk_sweep<T, DIM>(a);
-      --sp;
-      continue;
-    }
-    if (f.stage == 0) {
-      if (!f.skip_pre)
-        for (int s = 0; s < cp.nu1; ++s) blk_sweep<T, DIM>(a);
-      blk_restrict<T, DIM>(a, tab->l[f.lev + 1]);
-      f.stage = f.fcycle ? 1 : 2;
-      f.g = 0;
-    }
-    if (f.stage == 1) {  // F-cycle: gamma recursive F-cycles first (solver_2d.py:609-610)
-      if (f.g < cp.gamma) {
-        ++f.g;
-        st[sp++] = Frame{f.lev + 1, 0, 0, true, false};
-        continue;
-      }
-      f.stage = 2;
-      f.g = 0;
-    }
-    if (f.stage == 2) {  // gamma plain cycles (solver_2d.py:611)
-      if (f.g < cp.gamma) {
-        ++f.g;
-        st[sp++] = Frame{f.lev + 1, 0, 0, false, false};
-        continue;
-      }
-      f.stage = 3;
-    }
-    blk_prolong<T, DIM>(a, tab->l[f.lev + 1], cp.diag != 0);
-    for (int s = 0; s < cp.nu2; ++s) blk_sweep<T, DIM>(a);
-    --sp;
-  }
-}
-
 // The level table (~2 KB) is copied into shared memory first: every frame of the cycle
 // reads its level's pointers and sizes, and from the global table each of those reads
 // was an L2 round trip in front of the frame's first pass.

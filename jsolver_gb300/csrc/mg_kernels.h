@@ -108,6 +108,14 @@ size_t coarse_smem32_bytes(const int* mx, const int* my, int lev0, int last);
 int prepare_coarse_smem32(size_t bytes);
 void launch_coarse_smem32(const LvlTable<float>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
                           size_t smem, cudaStream_t s);
+// mg_coarse_staged.cu: the coarse sub-cycle on one block with every coarse array in shared
+// memory, staged by bulk copies (bytes from coarse_staged_bytes, 0 = does not fit;
+// prepare_coarse_staged: 0 = usable)
+size_t coarse_staged_bytes(int dim, const size_t* elems, int lev0, int last, size_t elem_size, bool offdiag);
+template <typename T> int prepare_coarse_staged(int dim, size_t bytes);
+template <typename T>
+void launch_coarse_staged(int dim, const LvlTable<T>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
+                          size_t smem, int threads, cudaStream_t s);
 // copies a level table into device memory (the coarse kernel reads it from there)
 template <typename T> void launch_store_table(const LvlTable<T>& tab, LvlTable<T>* dst, cudaStream_t s);
 

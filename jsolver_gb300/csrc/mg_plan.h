@@ -81,6 +81,11 @@ struct JmgPlan {
   // FP32 2D coarse levels from shared memory (k_coarse_smem32, opt-in JMG_COARSE32=smem):
   // its dynamic shared-memory bytes, 0 when not used
   size_t coarse_smem32 = 0;
+  // the single-block coarse sub-cycle with its levels staged in shared memory by bulk
+  // copies (mg_coarse_staged.cu, the default): dynamic shared-memory bytes of the FP64 and
+  // FP32 tables (0: the global-memory kernel instead) and the block size
+  size_t coarse_staged64 = 0, coarse_staged32 = 0;
+  int coarse_threads = 512;
 };
 
 

@@ -519,3 +519,60 @@ def test_mixed_coarse_from_shared_memory_matches_global(m, form, monkeypatch):
     phi_s, c_s = solve_2d(g, g, *args, **kw)
     assert int(c_s) == int(c_g)
     assert rel_l2(phi_s, phi_g) < 1e-13, rel_l2(phi_s, phi_g)
+
+
+STAGED_CASES = [(2, 1024, {"precision": "mixed", "outer": "fcg", "inner_cycles": 2}), (2, 256, {}),
+                (2, 256, {"gamma": 2}), (2, 256, {"fcycle": True}), (2, 128, {"skip_pre": True}),
+                (2, 128, {"nu1": 2, "nu2": 0}), (2, 128, {"nu1": 0, "nu2": 2}), (2, 512, {"precision": "mixed"}),
+                (2, 8, {}), (3, 32, {"fcycle": True}), (3, 64, {}), (3, 32, {"gamma": 2, "precision": "mixed"}),
+                (3, 64, {"precision": "mixed", "outer": "fcg", "fcycle": True})]
+
+
+@pytest.mark.parametrize("dim,m,form", STAGED_CASES,
+                         ids=lambda x: ",".join(f"{k}={v}" for k, v in x.items()) if isinstance(x, dict) else str(x))
+def test_staged_coarse_cycle_matches_global(dim, m, form, monkeypatch):
+    """The coarse sub-cycle with its levels staged in shared memory by bulk copies (the
+    default) against the global-memory single-block kernel (JMG_COARSE=global): the same
+    per-point functions on the same values, so the same bits and cycle counts."""
+    g = grid_1D(m)
+    if dim == 2:
+        p = W.random_2d(m, seed=23)
+        grids, fn = (g, g), solve_2d
+        args = (p["phi0"], p["rhs"], p["lam"], p["D_xx"], p["D_yy"])
+    else:
+        p = W.random_3d(m, seed=23)
+        grids, fn = (g, g, g), solve_3d
+        args = (p["phi0"], p["rhs"], p["lam"], p["D_xx"], p["D_yy"], p["D_zz"])
+    kw = dict(form)
+    if kw.get("precision") == "mixed" or kw.get("outer") == "fcg":
+        kw.update(stop="residual", rtol=1e-9)
+    else:
+        kw.update(fixed=True, max_iters_outer=5)
+    monkeypatch.setenv("JMG_COARSE", "global")
+    monkeypatch.setattr(_engine, "CACHE", _engine._Cache())
+    phi_g, c_g = fn(*grids, *args, **kw)
+    monkeypatch.delenv("JMG_COARSE")
+    monkeypatch.setattr(_engine, "CACHE", _engine._Cache())
+    phi_s, c_s = fn(*grids, *args, **kw)
+    assert int(c_s) == int(c_g)
+    np.testing.assert_array_equal(phi_s, phi_g)
+
+
+def test_staged_coarse_cycle_with_dxy(monkeypatch):
+    """The staged kernel with the four D_xy diagonal arrays per level."""
+    rng = np.random.default_rng(3)
+    m = 128
+    shape = (m + 3, m + 3)
+    dxx, dyy = np.exp(0.5 * rng.standard_normal(shape)), np.exp(0.5 * rng.standard_normal(shape))
+    dxy = 0.3 * np.minimum(dxx, dyy) * rng.uniform(-1, 1, shape)
+    args = (np.zeros(shape), rng.standard_normal(shape), rng.uniform(0, 5, shape), dxx, dyy)
+    g = grid_1D(m)
+    monkeypatch.setenv("JMG_COARSE", "global")
+    monkeypatch.setattr(_engine, "CACHE", _engine._Cache())
+    phi_g, c_g = solve_2d(g, g, *args, D_xy=dxy, fixed=True, max_iters_outer=4)
+    monkeypatch.delenv("JMG_COARSE")
+    monkeypatch.setattr(_engine, "CACHE", _engine._Cache())
+    phi_s, c_s = solve_2d(g, g, *args, D_xy=dxy, fixed=True, max_iters_outer=4)
+    np.testing.assert_array_equal(phi_s, phi_g)
+    ref, _ = mg2d.solve_2d(g, g, *args, D_xy=dxy, fixed=True, max_iters_outer=4)
+    assert rel_l2(phi_s, ref) < 1e-12
