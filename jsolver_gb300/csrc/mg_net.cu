@@ -22,9 +22,12 @@
 #include <cstring>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "../../include/jmg.h"
 #include "mg_kernels.h"
 #include "net_kernels.cuh"
+#include "net_tc.cuh"
 
 using jmgnet::bf16;
 
@@ -54,11 +57,56 @@ int grid_for(size_t n, int threads = 256) {
 
 // ---- convolution dispatch ----------------------------------------------------------------
 
+// The convolutions run on the tcgen05 kernel (net_tc.cuh) unless JMG_CONV=mma selects the
+// mma.sync kernel (net_kernels.cuh), which the tests compare it with.
+bool use_tcgen05() {
+  const char* e = getenv("JMG_CONV");
+  return !(e && std::strcmp(e, "mma") == 0);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
+}
+
+// tensor map of an NHWC BF16 activation [N][H][W][C]: boxes of 8 channels x 16 columns x
+// 10 rows of one image (an input tile with its halo, one 8-channel plane), zero fill
+bool activation_map(CUtensorMap* m, const bf16* X, int N, int H, int W, int C) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
+  const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+  const cuuint32_t box[4] = {8, (cuuint32_t)jmgnet::kTW, (cuuint32_t)jmgnet::kIH, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(X), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <int CIN, int COUT>
 void conv_t(const bf16* X, const bf16* W, const float* bias, const bf16* mask, bf16* Y, float* Y32, int N, int H,
-            int Wd, int relu, cudaStream_t s) {
-  using S = jmgnet::ConvSmem<CIN, COUT>;
+            int Wd, int relu, int* fault, cudaStream_t s) {
   const int tiles = N * (H / jmgnet::kTH) * (Wd / jmgnet::kTW);
+  CUtensorMap xmap;
+  if (use_tcgen05() && activation_map(&xmap, X, N, H, Wd, CIN)) {
+    using S = jmgnet::TcConv<CIN, COUT>;
+    // blocks per SM that shared memory (220 KB) and tensor memory (512 columns) allow
+    int per_sm = (220 * 1024) / S::smem;
+    if (per_sm > 512 / S::TCOLS) per_sm = 512 / S::TCOLS;
+    if (per_sm < 1) per_sm = 1;
+    const int blocks = tiles < 152 * per_sm ? tiles : 152 * per_sm;
+    jmgnet::k_conv3x3_tc<CIN, COUT><<<blocks, 128, S::smem, s>>>(xmap, W, bias, mask, Y, Y32, N, H, Wd, relu, fault);
+    return;
+  }
+  using S = jmgnet::ConvSmem<CIN, COUT>;
   const int blocks = tiles < 152 * 4 ? tiles : 152 * 4;
   jmgnet::k_conv3x3<CIN, COUT><<<blocks, 128, S::bytes, s>>>(X, W, bias, mask, Y, Y32, N, H, Wd, relu);
 }
@@ -81,6 +129,9 @@ int prep_t() {
   if (cudaFuncSetAttribute(jmgnet::k_conv3x3_wgrad<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            jmgnet::WgSmem<CIN, COUT>::bytes) != cudaSuccess)
     return 1;
+  if (cudaFuncSetAttribute(jmgnet::k_conv3x3_tc<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           jmgnet::TcConv<CIN, COUT>::smem) != cudaSuccess)
+    return 1;
   return 0;
 }
 
@@ -95,10 +146,10 @@ int prepare_all() {
 }
 
 bool conv(int cin, int cout, const bf16* X, const bf16* W, const float* bias, const bf16* mask, bf16* Y, float* Y32,
-          int N, int H, int Wd, int relu, cudaStream_t s) {
+          int N, int H, int Wd, int relu, int* fault, cudaStream_t s) {
 #define C_(a, b)                                                      \
   if (cin == a && cout == b) {                                        \
-    conv_t<a, b>(X, W, bias, mask, Y, Y32, N, H, Wd, relu, s);        \
+    conv_t<a, b>(X, W, bias, mask, Y, Y32, N, H, Wd, relu, fault, s); \
     return true;                                                      \
   }
   JMG_NET_SHAPES(C_)
@@ -306,6 +357,7 @@ struct JmgNet {
   float* rms = nullptr;
   float* loss_scratch = nullptr;
   double* ritz_parts = nullptr;
+  int* fault = nullptr;     // set by a tcgen05 convolution whose wait ran out
   std::vector<void*> allocs;
 
   template <typename T>
@@ -339,7 +391,7 @@ void forward(JmgNet* n, const bf16* x, int B, cudaStream_t s) {
     const LayerDesc& d = kNet[l];
     const int r = R >> d.lev;
     conv(d.cin, d.cout, in, n->wb + n->wpos[l], n->params + w_off(l) + w_elems(l), nullptr, out, out32, B, r, r,
-         d.relu, s);
+         d.relu, n->fault, s);
   };
   auto pool = [&](const bf16* in, bf16* out, int lev, int C) {
     const int r = R >> lev;
@@ -385,7 +437,7 @@ void backward(JmgNet* n, const bf16* x, const float* target, int B, float* loss,
     jmgnet::k_bias_grad<<<dim3(grid_for(np) > 64 ? 64 : grid_for(np), d.cout), 256, 0, s>>>(gout, gw + w_elems(l), np,
                                                                                              d.cout);
     if (gin)
-      conv(d.cout, d.cin, gout, n->wt + n->wpos[l], nullptr, mask, gin, nullptr, B, r, r, 0, s);
+      conv(d.cout, d.cin, gout, n->wt + n->wpos[l], nullptr, mask, gin, nullptr, B, r, r, 0, n->fault, s);
   };
   auto upbwd = [&](const bf16* gu, const bf16* mask, bf16* gc, int lev, int C) {
     const int r = R >> lev;
@@ -480,12 +532,12 @@ int jmg_net_create(JmgNet** out, int res, int max_batch) {
   ok = ok && (n->y32 = n->alloc<float>(n->pix(0, B) * 16)) && (n->gy = n->alloc<bf16>(n->pix(0, B) * 16)) &&
        (n->x1 = n->alloc<bf16>(n->pix(0, 1) * 16)) && (n->tmp = n->alloc<float>(n->pix(0, 1) * 4)) &&
        (n->rms = n->alloc<float>(1)) && (n->loss_scratch = n->alloc<float>(1)) &&
-       (n->ritz_parts = n->alloc<double>(2 * kRitzBlocks));
+       (n->ritz_parts = n->alloc<double>(2 * kRitzBlocks)) && (n->fault = n->alloc<int>(1));
   if (!ok) {
     jmg_net_destroy(n);
     return jmg::set_error_message(JMG_ERR_CUDA, "cudaMalloc failed while creating the network");
   }
-  if (cudaMemset(n->params, 0, P * sizeof(float)) != cudaSuccess || cudaMemset(n->adam_m, 0, P * 4) != cudaSuccess ||
+  if (cudaMemset(n->fault, 0, sizeof(int)) != cudaSuccess || cudaMemset(n->params, 0, P * sizeof(float)) != cudaSuccess || cudaMemset(n->adam_m, 0, P * 4) != cudaSuccess ||
       cudaMemset(n->adam_v, 0, P * 4) != cudaSuccess) {
     jmg_net_destroy(n);
     return cuda_check("cudaMemset");

@@ -141,3 +141,30 @@ def test_trained_guess_against_zero_guess(m):
         learned.append(int(c1))
     print(f"m={m}: guess rel. error {np.median(err):.3f}; cycles zero {zero} learned {learned}")
     assert np.median(err) < 1.0  # the Ritz-scaled guess is closer to phi than zero is
+
+
+@pytest.mark.parametrize("res,B", [(128, 2), (256, 8)])
+def test_tcgen05_convolutions_match_mma_sync(res, B, monkeypatch):
+    """The convolutions on the 5th-generation tensor cores (tcgen05.mma into tensor memory,
+    TMA input tiles; the default) against the mma.sync kernels (JMG_CONV=mma): the same
+    network output and gradients up to the order of the FP32 sums, which flips an
+    occasional BF16 rounding of a stored activation (forward 5e-3, gradients 2e-2
+    relative L2)."""
+    p = _params(5)
+    xo, xg = _inputs(B, res, 6)
+    t = torch.from_numpy(np.random.default_rng(7).standard_normal((B, res, res)).astype(np.float32)).to(DEV)
+    out = {}
+    for kind in ("mma", "tc"):
+        if kind == "mma":
+            monkeypatch.setenv("JMG_CONV", "mma")
+        else:
+            monkeypatch.delenv("JMG_CONV", raising=False)
+        net = LN.GuessNet(res=res, max_batch=B, device=DEV, params=p)
+        y = net.forward(xg).cpu().numpy()
+        loss, g = net.loss_grad(xg, t)
+        out[kind] = (y, float(loss), g.cpu().numpy())
+    (y0, l0, g0), (y1, l1, g1) = out["mma"], out["tc"]
+    assert rel(y1, y0) < 5e-3, rel(y1, y0)
+    assert abs(l1 - l0) <= 1e-3 * abs(l0)
+    for li, ((ws, we), (bs, be)) in enumerate(U.layer_slices()):
+        assert rel(g1[ws:we], g0[ws:we]) < 2e-2, (li, rel(g1[ws:we], g0[ws:we]))
