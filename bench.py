@@ -24,7 +24,8 @@ public API (solve_2d / solve_3d on CUDA tensors) with the host->device copies of
 inputs from pinned memory and the device->host copy of phi and the count inside the
 timed region. ``roofline`` is the kernel with the largest share of the solve in the
 committed launch list (profiles/launch_shares.json), timed alone with CUDA events;
-``roofline_fine_sweep`` the fine-level sweep beside it. ``cpu_baseline`` is the median
+``roofline_fine`` the fine-level kernel beside it (the fused smooth + restrict launch where level 0
+runs the fused pairs, else the sweep). ``cpu_baseline`` is the median
 time of full solves of the C oracle on all host cores. ``--gpus N`` under torchrun runs
 N independent replicas (the path does not shard).
 
@@ -589,6 +590,21 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
                       "peak": peak, "unit": "GB/s", "peak_source": peak_src,
                       "alg_bytes_per_launch": alg_sweep / launches_per_sweep,
                       "launch_ms": sweep_ms / launches_per_sweep, "traffic": traffic}
+        if dim == 2 and lib.jmg_plan_level_fused(plan.handle, 0, fp32):
+            # level 0 runs the fused pairs: time its smooth + restrict launch (reads phi, rhs,
+            # the two face arrays, 1/A_cc and A_cc; writes phi's second buffer and the coarse
+            # rhs and phi: (7 N0 + 2 Nc) * s bytes)
+            sr = lambda s_: _lib.check(lib.jmg_op_smooth_restrict_ws(plan.handle, 0, fp32, *wsa,  # noqa: E731
+                                                                     vp(s_.cuda_stream)))
+            sr(stream)
+            sr_ms = timed_alone(sr, stream, flush, 20)
+            alg_sr = (7 * n0 + 2 * (m // 2 + 3) ** 2) * elem
+            roof_sweep = {"bound": "hbm", "kernel": f"k_smooth_restrict2d<{'float' if fp32 else 'double'}> (level 0: "
+                                                     "last pre-sweep + defect + restriction, one launch)",
+                          "achieved": alg_sr / (sr_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                          "peak_source": peak_src, "alg_bytes_per_launch": alg_sr, "launch_ms": sr_ms,
+                          "traffic": load_json("profiles/traffic.json").get(
+                              f"smooth_restrict_{'fp32' if fp32 else 'fp64'}_2d_{m}")}
         roof_sweep["frac"] = roof_sweep["achieved"] / peak
         # the coarse sub-cycle (one launch from the first coarse level down)
         lib.jmg_op_coarse_ws(plan.handle, fp32, *wsa, vp(stream.cuda_stream))
@@ -603,7 +619,8 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
                                                  f"^{dim} in one launch; latency-bound, its arrays stay in L2)",
                        "achieved": alg_coarse / (coarse_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                        "peak_source": peak_src, "alg_bytes_per_launch": alg_coarse, "launch_ms": coarse_ms,
-                       "traffic": None}
+                       "traffic": load_json("profiles/traffic.json").get(
+                           f"coarse_{'fp32' if fp32 else 'fp64'}_{dim}d_{m}")}
         roof_coarse["frac"] = roof_coarse["achieved"] / peak
 
         # end to end through the public API from pinned host buffers
@@ -644,11 +661,11 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
 
     # the kernel with the largest share of the solve in the committed launch list
     shares = load_json("profiles/launch_shares.json").get(f"{dim}d_{m}_{args.form}_{args.outer}_{cycle}", {})
-    dominant = "coarse" if shares.get("coarse", 0.0) > shares.get("fine_sweep", 0.0) else "fine_sweep"
+    dominant = "coarse" if shares.get("coarse", 0.0) > shares.get("fine", 0.0) else "fine"
     roof = dict(roof_coarse if dominant == "coarse" else roof_sweep)
     roof["launch_share"] = shares.get(dominant)
     roof_other = dict(roof_sweep if dominant == "coarse" else roof_coarse)
-    roof_other["launch_share"] = shares.get("fine_sweep" if dominant == "coarse" else "coarse")
+    roof_other["launch_share"] = shares.get("fine" if dominant == "coarse" else "coarse")
 
     line = {
         "metric": metric_name(dim, m), "value": ms, "unit": "ms", "n_gpus": ws_n, "steps": steps,
@@ -669,7 +686,7 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
         "learned_guess_form": learned_cmp,
         "max_err_vs_exact_discrete": err_exact,
         "roofline": roof,
-        "roofline_fine_sweep" if dominant == "coarse" else "roofline_coarse": roof_other,
+        "roofline_fine" if dominant == "coarse" else "roofline_coarse": roof_other,
         "e2e": ({"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
                 if e2e_ms is not None else None),
         "gpu_launches": int(launches),

@@ -237,6 +237,18 @@ int jmg_op_coarse_ws(JmgPlan* plan, int fp32, void* workspace, size_t workspace_
  * counterpart. */
 int jmg_plan_coarse_start(const JmgPlan* plan);
 
+/* Whether this plan's solves run the fused operator pairs on a 2D level (fp32 != 0: the
+ * FP32 cycles of a mixed plan): the last pre-sweep with the defect and restriction, the
+ * prolongation with the first post-sweep, each one launch over tiles with halos. No
+ * reference counterpart. */
+int jmg_plan_level_fused(const JmgPlan* plan, int level, int fp32);
+/* The last pre-sweep of a level followed by defect + restriction onto level + 1
+ * (red_black_gauss_seidel then defect, solver_2d.py:670-692, 616-647) on the arrays
+ * already in the workspace, as a solve runs them (one fused launch where
+ * jmg_plan_level_fused says so), for timing them alone. No reference counterpart. */
+int jmg_op_smooth_restrict_ws(JmgPlan* plan, int level, int fp32, void* workspace, size_t workspace_bytes,
+                              jmg_stream_t stream);
+
 /* Kernel launches per sweep of a level in this plan's solves (fp32 != 0: the FP32
  * cycles of a mixed plan): 1 for the one-pass 3D sweep, 2 colour passes, 4 sub-lattice
  * passes with D_xy; 0 for a bad level. No reference counterpart. */

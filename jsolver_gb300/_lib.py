@@ -68,6 +68,8 @@ _SIGS = {
     "jmg_op_smooth32_ws": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_size_t, _P]),
     "jmg_op_coarse_ws": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t, _P]),
     "jmg_plan_coarse_start": (ctypes.c_int, [_P]),
+    "jmg_plan_level_fused": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
+    "jmg_op_smooth_restrict_ws": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_size_t, _P]),
     "jmg_plan_launch_counts": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
     "jmg_rel_residual_noalloc": (ctypes.c_int, [ctypes.POINTER(JmgGrid), _P, _P, ctypes.POINTER(JmgCoeffs), _P, _P]),
     "jmg_adjoint_workspace_bytes": (ctypes.c_size_t, [_P]),

@@ -1164,6 +1164,38 @@ int jmg_op_coarse_ws(JmgPlan* p, int fp32, void* ws, size_t bytes, jmg_stream_t 
 
 int jmg_plan_coarse_start(const JmgPlan* p) { return p ? p->coarse_start : -1; }
 
+int jmg_plan_level_fused(const JmgPlan* p, int level, int fp32) {
+  if (!p || level < 0 || level + 1 >= p->used) return 0;
+  const LevelInfo& li = p->lv[level];
+  return li.fuse_ops && (fp32 ? li.phi2_32 != 0 : li.phi2 != 0) ? 1 : 0;
+}
+
+int jmg_op_smooth_restrict_ws(JmgPlan* p, int level, int fp32, void* ws, size_t bytes, jmg_stream_t stream) {
+  int rc = check_ws(p, ws, bytes);
+  if (rc || (rc = level_check(p, level, true))) return rc;
+  if (fp32 && !p->mixed) return set_err(JMG_ERR_VALUE, "jmg_op_smooth_restrict_ws(fp32=1) needs a plan with precision mixed");
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool fused = jmg_plan_level_fused(p, level, fp32) != 0;
+  if (fused && (rc = coarse_setup(p))) return rc;  // the fused kernels' attributes
+  if (fp32) {
+    Lvl<float> f = lvl32(p, ws, level), c = lvl32(p, ws, level + 1);
+    if (fused) launch_smooth_restrict2d<float>(f, c, false, s);
+    else {
+      launch_sweep<float>(p->dim, f, s);
+      launch_restrict<float>(p->dim, f, c, s);
+    }
+  } else {
+    Lvl<double> f = lvl64(p, ws, level), c = lvl64(p, ws, level + 1);
+    if (fused) launch_smooth_restrict2d<double>(f, c, false, s);
+    else {
+      launch_sweep<double>(p->dim, f, s);
+      launch_restrict<double>(p->dim, f, c, s);
+    }
+  }
+  JMG_CUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
 int jmg_plan_sweep_launches(const JmgPlan* p, int level, int fp32) {
   if (!p || level < 0 || level >= p->used) return 0;
   const LevelInfo& li = p->lv[level];
