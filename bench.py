@@ -614,9 +614,10 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
         cf = _engine.make_config(**opts)
         alg_coarse = coarse_alg_bytes(dim, m, plan.levels, cstart, max(cf.gamma, 1), max(cf.nu1, 0), max(cf.nu2, 0),
                                       elem)
-        roof_coarse = {"bound": "hbm", "kernel": f"k_coarse_cycle<{'float' if fp32 else 'double'}, {dim}> "
+        coarse_name = "k_coarse_cycle" if os.environ.get("JMG_COARSE") else "k_coarse_staged"
+        roof_coarse = {"bound": "hbm", "kernel": f"{coarse_name}<{'float' if fp32 else 'double'}, {dim}> "
                                                  f"(1 block: levels {m >> cstart}^{dim} ... {m >> (plan.levels - 2)}"
-                                                 f"^{dim} in one launch; latency-bound, its arrays stay in L2)",
+                                                 f"^{dim} in one launch, staged in shared memory; latency-bound)",
                        "achieved": alg_coarse / (coarse_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                        "peak_source": peak_src, "alg_bytes_per_launch": alg_coarse, "launch_ms": coarse_ms,
                        "traffic": load_json("profiles/traffic.json").get(
