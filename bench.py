@@ -51,6 +51,7 @@ WORKLOADS = {  # name -> (dimension, default resolution, default cycle)
     "2d": (2, 1024, "V"),  # 2D 1024^2 random-coefficient problem (arrays 1027^2 float64)
     "3d": (3, 256, "F"),   # 3D 256^3 random-coefficient problem (arrays 259^3 float64)
     "adjoint": (2, 512, "V"),  # reverse mode: 2D 512^2, fixed 12 V-cycles, loss sum(w phi)
+    "adjoint3d": (3, 64, "V"),  # reverse mode: 3D 64^3, fixed 12 V-cycles, loss sum(w phi)
     "batch": (2, 256, "V"),  # many independent 2D 256^2 problems in one batched call
 }
 
@@ -81,6 +82,7 @@ def parse():
     ap.add_argument("--no-3d", action="store_true", help="default run: skip the 3D 256^3 block (workload_3d)")
     ap.add_argument("--batch", type=int, default=64, help="problems per step of the batch workload")
     ap.add_argument("--iters", type=int, default=12, help="fixed cycles of the adjoint workload")
+    ap.add_argument("--dxy", action="store_true", help="adjoint workload: with D_xy (2D 9-point stencil)")
     ap.add_argument("--lanes", type=int, default=8, help="concurrent lanes of the batch workload")
     a = ap.parse_args()
     dim, m, cyc = WORKLOADS[a.workload]
@@ -278,21 +280,33 @@ def workload_name(dim, m):
 
 
 def adjoint_bench(args):
-    """Reverse mode of the fixed-mode 2D solve: forward (--iters V-cycles, 12 by default) and backward (the
-    hand-written adjoint) device times, their ratio and the peak device memory of one
-    forward + backward, on the 2D random-coefficient problem at 512^2, loss = sum(w phi)
-    with seeded Gaussian weights w."""
+    """Reverse mode of the fixed-mode solve: forward (--iters V-cycles, 12 by default) and
+    backward (the hand-written adjoint) device times, their ratio and the peak device memory
+    of one forward + backward, loss = sum(w phi) with seeded Gaussian weights w: the 2D
+    random-coefficient problem at 512^2 (workload adjoint; --dxy adds a D_xy field of
+    |D_xy| <= 0.3 min(D_xx, D_yy)), or the 3D one at 64^3 (workload adjoint3d)."""
     import torch
     from jsolver_gb300 import workloads
     from jsolver_gb300.grid_1d import grid_1D
     from jsolver_gb300.solver_2d import solve_2d
+    from jsolver_gb300.solver_3d import solve_3d
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    m, iters = args.m, args.iters
-    p = workloads.random_2d(m, seed=args.seed)
+    m, iters, dim = args.m, args.iters, args.dim
+    p = make_problem(args, args.seed)
     g = grid_1D(m)
     w = torch.from_numpy(np.random.default_rng(args.seed + 1).standard_normal(p["rhs"].shape)).to(dev)
-    names = ("phi0", "rhs", "lam", "D_xx", "D_yy")
+    names = ["phi0", "rhs", "lam"] + coeff_names(dim)
+    dxy = dim == 2 and args.dxy
+    if dxy:
+        u = np.random.default_rng(args.seed + 2).uniform(-1, 1, p["rhs"].shape)
+        p["D_xy"] = 0.3 * np.minimum(p["D_xx"], p["D_yy"]) * u
+        names.append("D_xy")
+
+    def solve(x, **kw):
+        if dim == 3:
+            return solve_3d(g, g, g, *x, **kw)
+        return solve_2d(g, g, *x[:5], D_xy=x[5] if dxy else None, **kw)
 
     def inputs(grad):
         return [torch.from_numpy(p[k]).to(dev).requires_grad_(grad and k != "phi0") for k in names]
@@ -304,10 +318,10 @@ def adjoint_bench(args):
         e0, e1 = ev(), ev()
         e0.record()
         with torch.no_grad():
-            solve_2d(g, g, *x, fixed=True, max_iters_outer=iters)
+            solve(x, fixed=True, max_iters_outer=iters)
         e1.record()
         x = inputs(True)
-        phi, _ = solve_2d(g, g, *x, fixed=True, max_iters_outer=iters)
+        phi, _ = solve(x, fixed=True, max_iters_outer=iters)
         loss = (phi * w).sum()
         e2, e3 = ev(), ev()
         e2.record()
@@ -326,16 +340,19 @@ def adjoint_bench(args):
     torch.cuda.reset_peak_memory_stats(dev)
     base = torch.cuda.memory_allocated(dev)
     x = inputs(True)
-    phi, _ = solve_2d(g, g, *x, fixed=True, max_iters_outer=iters)
+    phi, _ = solve(x, fixed=True, max_iters_outer=iters)
     (phi * w).sum().backward()
     torch.cuda.synchronize()
     peak = torch.cuda.max_memory_allocated(dev) - base
     f, b = float(np.median(fwd)), float(np.median(bwd))
-    line = {"metric": f"backward/forward time ratio, reverse mode of the fixed-mode 2D solve ({m}^2, {iters} V-cycles)",
+    stencil = " with D_xy" if dxy else ""
+    line = {"metric": f"backward/forward time ratio, reverse mode of the fixed-mode {dim}D solve{stencil} "
+                      f"({m}^{dim}, {iters} V-cycles)",
             "value": b / f, "unit": "ratio", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": False, "dtype": "f64", "data": "synthetic (seeded GRF coefficients, manufactured rhs)",
-            "config": {"workload": f"2d-{m}^2-random-coeff fixed {iters} V-cycles, loss = sum(w phi)",
-                       "gradients": "rhs, lam, D_xx, D_yy (and phi0)"},
+            "config": {"workload": f"{dim}d-{m}^{dim}-random-coeff{stencil} fixed {iters} V-cycles, "
+                                   f"loss = sum(w phi)",
+                       "gradients": ", ".join(names[1:]) + " (and phi0)"},
             "forward_ms": f, "backward_ms": b, "peak_device_memory_mb": peak / 2 ** 20,
             "array_mb": p["rhs"].nbytes / 2 ** 20}
     print(json.dumps(line), flush=True)
@@ -702,7 +719,7 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
 
 def main():
     args = parse()
-    if args.workload == "adjoint":
+    if args.workload in ("adjoint", "adjoint3d"):
         return adjoint_bench(args)
     if args.workload == "batch":
         return batch_bench(args)

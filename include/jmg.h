@@ -192,6 +192,15 @@ int jmg_solve_fixed_vjp(JmgPlan* plan, const double* phi0, const double* rhs, co
                         const double* phi_bar, double* phi0_bar, double* rhs_bar, double* lam_bar,
                         double* Dxx_bar, double* Dyy_bar, void* workspace, size_t workspace_bytes,
                         void* adjoint_workspace, size_t adjoint_workspace_bytes, jmg_stream_t stream);
+/* Reverse mode of the fixed-mode solve in 2D and 3D, with the 5-, 7- or 9-point stencil:
+ * jax.vjp of solve_2d / solve_3d with fixed = True (solver_2d.py:461-463, solver_3d.py:
+ * 468-470). D_bar holds one output per axis (dL/dD_xx, dL/dD_yy[, dL/dD_zz]); Dxy_bar is
+ * dL/dD_xy for a plan created with off_diag (NULL otherwise). The other arguments are those
+ * of jmg_solve_fixed_vjp, which is this function for 2D plans without D_xy. */
+int jmg_solve_fixed_vjp_nd(JmgPlan* plan, const double* phi0, const double* rhs, const JmgCoeffs* coeffs,
+                           const double* phi_bar, double* phi0_bar, double* rhs_bar, double* lam_bar,
+                           double* const* D_bar, double* Dxy_bar, void* workspace, size_t workspace_bytes,
+                           void* adjoint_workspace, size_t adjoint_workspace_bytes, jmg_stream_t stream);
 
 /* Forward mode of the solve (jax.jvp through solve_2d / solve_3d: through the fixed
  * fori_loop, solver_2d.py:461-463, and through the dynamic while_loop, solver_2d.py:465-477,

@@ -199,11 +199,11 @@ def solve(grids, phi, rhs, lam, D, D_xy=None, guess=None, **opts):
         if not cfg.fixed:
             raise ValueError("reverse-mode differentiation needs fixed=True, as in the reference "
                              "(its dynamic while_loop is not reverse-differentiable)")
-        if ndim != 2 or cfg.precision != _lib.PREC_FP64 or off or cfg.outer != _lib.OUTER_RICHARDSON:
-            raise NotImplementedError("the hand-written adjoint covers the 2D FP64 fixed-mode solve of the "
-                                      "5-point stencil (no D_xy), iterated as in the reference")
-        from .adjoint import solve_2d_fixed_diff
-        return solve_2d_fixed_diff(grids, phi, rhs, lam, D[0], D[1], **opts)
+        if cfg.precision != _lib.PREC_FP64 or cfg.outer != _lib.OUTER_RICHARDSON:
+            raise NotImplementedError("the hand-written adjoint differentiates the reference's FP64 fixed-mode "
+                                      "iteration (precision fp64, outer richardson)")
+        from .adjoint import solve_fixed_diff
+        return solve_fixed_diff(grids, phi, rhs, lam, D, D_xy if off else None, **opts)
     device = pick_device(phi, rhs, lam, *D)
     _lib.load()
     with torch.cuda.device(device):

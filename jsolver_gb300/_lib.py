@@ -80,6 +80,8 @@ _SIGS = {
                                      _P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, _P]),
     "jmg_solve_fixed_vjp": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(JmgCoeffs), _P, _P, _P, _P, _P, _P, _P,
                                            ctypes.c_size_t, _P, ctypes.c_size_t, _P]),
+    "jmg_solve_fixed_vjp_nd": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(JmgCoeffs), _P, _P, _P, _P,
+                                              ctypes.POINTER(_P), _P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, _P]),
     "jmg_net_num_params": (ctypes.c_int64, []),
     "jmg_net_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int]),
     "jmg_net_destroy": (None, [_P]),

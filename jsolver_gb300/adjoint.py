@@ -1,12 +1,14 @@
-"""Differentiation of the solve: reverse mode of the fixed-mode 2D solve (torch.autograd)
-and forward mode of every solve (jvp, torch.func.jvp).
+"""Differentiation of the solve: reverse mode of the fixed-mode solve (torch.autograd) and
+forward mode of every solve (jvp, torch.func.jvp).
 
-The reference differentiates ``solve_2d(..., fixed=True)`` with ``jax.vjp``
-(jsolver/solver_2d.py:18-26; README: reverse mode works in fixed mode only). Here the
-vector-Jacobian product is the hand-written adjoint in libjmg (``jmg_solve_fixed_vjp``:
-transposed smoother, restriction and prolongation swapped, per-cycle checkpointing with
-recomputation, backward of the coefficient hierarchy). ``solve_2d`` routes CUDA tensors
-that require grad through ``FixedSolve2D`` when ``fixed=True``.
+The reference differentiates ``solve_2d(..., fixed=True)`` and ``solve_3d(..., fixed=True)``
+with ``jax.vjp`` (jsolver/solver_2d.py:18-26, solver_3d.py:468-470; README: reverse mode
+works in fixed mode only). Here the vector-Jacobian product is the hand-written adjoint in
+libjmg (``jmg_solve_fixed_vjp_nd``: transposed smoother, restriction and prolongation
+swapped, per-cycle checkpointing with recomputation, backward of the coefficient
+hierarchy), for 2D and 3D and the 5-, 7- and 9-point (D_xy) stencils. ``solve_2d`` and
+``solve_3d`` route CUDA tensors that require grad through ``FixedSolve`` when
+``fixed=True``.
 """
 import ctypes
 
@@ -19,61 +21,77 @@ def _vp(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
-class FixedSolve2D(torch.autograd.Function):
-    """phi_n = solve_2d(grid_x, grid_y, phi0, rhs, lam, D_xx, D_yy, fixed=True, ...)."""
+def _full(x, shape):
+    return x.expand(shape).contiguous() if x.dim() == 0 else x.contiguous()
+
+
+class FixedSolve(torch.autograd.Function):
+    """phi_n = solve(grids, phi0, rhs, lam, D[, D_xy], fixed=True, ...) with
+    xs = (phi0, rhs, lam, D_xx, D_yy[, D_zz][, D_xy])."""
 
     @staticmethod
-    def forward(ctx, phi0, rhs, lam, D_xx, D_yy, grids, opts):
-        shape = phi0.shape
-        lam_a = lam.expand(shape).contiguous() if lam.dim() == 0 else lam.contiguous()
-        Dx = D_xx.expand(shape).contiguous() if D_xx.dim() == 0 else D_xx.contiguous()
-        Dy = D_yy.expand(shape).contiguous() if D_yy.dim() == 0 else D_yy.contiguous()
-        phi0 = phi0.contiguous()
-        rhs = rhs.contiguous()
+    def forward(ctx, grids, opts, has_dxy, *xs):
+        ndim = len(grids)
+        shape = xs[0].shape
+        phi0, rhs = xs[0].contiguous(), xs[1].contiguous()
+        lam = _full(xs[2], shape)
+        D = tuple(_full(d, shape) for d in xs[3:3 + ndim])
+        Dxy = xs[3 + ndim].contiguous() if has_dxy else None
         with torch.no_grad():
-            phi, _ = _engine.solve(grids, phi0, rhs, lam_a, (Dx, Dy), None, **opts)
-        ctx.save_for_backward(phi0, rhs, lam_a, Dx, Dy)
-        ctx.grids, ctx.opts = grids, opts
-        ctx.lam_scalar, ctx.dx_scalar, ctx.dy_scalar = lam.dim() == 0, D_xx.dim() == 0, D_yy.dim() == 0
+            phi, _ = _engine.solve(grids, phi0, rhs, lam, D, Dxy, **opts)
+        ctx.save_for_backward(phi0, rhs, lam, *D, *([Dxy] if has_dxy else []))
+        ctx.grids, ctx.opts, ctx.has_dxy = grids, opts, has_dxy
+        ctx.scalar = [x.dim() == 0 for x in xs]
         return phi
 
     @staticmethod
     def backward(ctx, gphi):
-        phi0, rhs, lam, Dx, Dy = ctx.saved_tensors
+        saved = ctx.saved_tensors
+        ndim = len(ctx.grids)
+        phi0, rhs, lam = saved[:3]
+        D = saved[3:3 + ndim]
         lib = _lib.load()
-        plan = _engine.CACHE.plan(_engine.make_grid(ctx.grids), _engine.make_config(**ctx.opts))
+        cfg = _engine.make_config(off_diag=ctx.has_dxy, **ctx.opts)
+        plan = _engine.CACHE.plan(_engine.make_grid(ctx.grids), cfg)
         dev = phi0.device
         ws = _engine.CACHE.workspace(plan, dev)
         abytes = lib.jmg_adjoint_workspace_bytes(plan.handle)
         aws = _engine.CACHE.workspace(plan, dev, "adjoint", abytes)
         co = _lib.JmgCoeffs()
         co.lam = lam.data_ptr()
-        co.D[0], co.D[1] = Dx.data_ptr(), Dy.data_ptr()
-        outs = [torch.empty_like(phi0) for _ in range(5)]
+        for a, d in enumerate(D):
+            co.D[a] = d.data_ptr()
+        co.D_xy = saved[3 + ndim].data_ptr() if ctx.has_dxy else None
+        outs = [torch.empty_like(phi0) for _ in range(3 + ndim + (1 if ctx.has_dxy else 0))]
+        dbar = (ctypes.c_void_p * 3)(*[o.data_ptr() for o in outs[3:3 + ndim]])
         gphi = gphi.contiguous().to(torch.float64)
-        _lib.check(lib.jmg_solve_fixed_vjp(plan.handle, _vp(phi0), _vp(rhs), ctypes.byref(co), _vp(gphi),
-                                           *[_vp(o) for o in outs], _vp(ws), ctypes.c_size_t(ws.numel()), _vp(aws),
-                                           ctypes.c_size_t(aws.numel()),
-                                           ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)))
-        g0, grhs, glam, gdx, gdy = outs
-        if ctx.lam_scalar:
-            glam = glam.sum()
-        if ctx.dx_scalar:
-            gdx = gdx.sum()
-        if ctx.dy_scalar:
-            gdy = gdy.sum()
-        return g0, grhs, glam, gdx, gdy, None, None
+        _lib.check(lib.jmg_solve_fixed_vjp_nd(
+            plan.handle, _vp(phi0), _vp(rhs), ctypes.byref(co), _vp(gphi), _vp(outs[0]), _vp(outs[1]),
+            _vp(outs[2]), dbar, _vp(outs[3 + ndim]) if ctx.has_dxy else None, _vp(ws), ctypes.c_size_t(ws.numel()),
+            _vp(aws), ctypes.c_size_t(aws.numel()), ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)))
+        # a scalar input's gradient is the sum over the array it stood for
+        grads = [o.sum() if sc else o for o, sc in zip(outs, ctx.scalar)]
+        return (None, None, None, *grads)
+
+
+def solve_fixed_diff(grids, phi0, rhs, lam, D, D_xy=None, **opts):
+    """Differentiable fixed-mode solve (2D or 3D, optional D_xy) on CUDA tensors; returns
+    (phi, count)."""
+    if not opts.get("fixed", False):
+        raise ValueError("reverse-mode differentiation needs fixed=True, as in the reference")
+    args = [phi0, rhs, lam, *D] + ([D_xy] if D_xy is not None else [])
+    dev = next(t.device for t in args if isinstance(t, torch.Tensor))
+
+    def T(x):
+        return x if isinstance(x, torch.Tensor) else torch.as_tensor(x, dtype=torch.float64, device=dev)
+
+    phi = FixedSolve.apply(tuple(grids), dict(opts), D_xy is not None, *[T(a) for a in args])
+    return phi, int(opts.get("max_iters_outer"))
 
 
 def solve_2d_fixed_diff(grids, phi0, rhs, lam, D_xx, D_yy, **opts):
-    """Differentiable fixed-mode 2D solve on CUDA tensors; returns (phi, count)."""
-    if not opts.get("fixed", False):
-        raise ValueError("reverse-mode differentiation needs fixed=True, as in the reference")
-    dev = next(t.device for t in (phi0, rhs, lam, D_xx, D_yy) if isinstance(t, torch.Tensor))
-    def T(x):
-        return x if isinstance(x, torch.Tensor) else torch.as_tensor(x, dtype=torch.float64, device=dev)
-    phi = FixedSolve2D.apply(T(phi0), T(rhs), T(lam), T(D_xx), T(D_yy), tuple(grids), dict(opts))
-    return phi, int(opts.get("max_iters_outer"))
+    """The 2D 5-point form of ``solve_fixed_diff``."""
+    return solve_fixed_diff(grids, phi0, rhs, lam, (D_xx, D_yy), **opts)
 
 
 # ---- forward mode ----------------------------------------------------------------------

@@ -1,14 +1,17 @@
-// mg_adjoint.cu — hand-written reverse mode of the fixed-mode 2D solve (vector-Jacobian
-// product), with per-cycle checkpointing and recomputation.
+// mg_adjoint.cu — hand-written reverse mode of the fixed-mode solve (vector-Jacobian
+// product) in 2D (5- and 9-point stencils) and 3D, with per-cycle checkpointing and
+// recomputation.
 //
-// The reference's fixed mode (solver_2d.py:461-463) is differentiated with jax.vjp, which
-// tapes every cycle (memory grows with cycles x grid, performance.md:44-60). Here:
+// The reference's fixed mode (solver_2d.py:461-463, solver_3d.py:468-470) is
+// differentiated with jax.vjp, which tapes every cycle (memory grows with cycles x grid,
+// performance.md:44-60). Here:
 //   forward:  phi_0 (do_BCs) -> n cycles, keeping only phi at the start of every cycle;
 //   backward: for k = n-1 .. 0: re-run cycle k from its checkpoint with per-operator
 //             snapshots of phi, then apply the transposed operators in reverse order
 //             (mg_adjoint_kernels.cu): colour updates reversed, restriction <-> prolongation
 //             transposed; finally the backward of the coefficient hierarchy.
-// Outputs: adjoints of phi0, rhs, lambda, D_xx, D_yy (dense arrays, like the inputs). The
+// Outputs: adjoints of phi0, rhs, lambda, the D components and D_xy (dense arrays, like
+// the inputs). The
 // frame of phi is reset by do_BCs at every sweep and cycle, so its adjoint there is zero.
 // The checkpointed forward and the reverse sweep are captured once into a CUDA graph per
 // (workspace, adjoint workspace) pair. Within a cycle, each run of operators on the small
@@ -29,13 +32,19 @@
 
 namespace jmg {
 
-void adj_sweep(const Lvl<double>& a, const AdjLvl& g, const double* before, const double* after, cudaStream_t s);
-void adj_restrict(const Lvl<double>& a, const AdjLvl& g, const double* phi, const Lvl<double>& c, const AdjLvl& gc,
-                  cudaStream_t s);
-void adj_prolong(const Lvl<double>& f, const AdjLvl& gf, const Lvl<double>& c, const AdjLvl& gc, int diag,
+void adj_sweep(int dim, const Lvl<double>& a, const AdjLvl& g, const double* before, const double* after,
+               cudaStream_t s);
+void adj_restrict(int dim, const Lvl<double>& a, const AdjLvl& g, const double* phi, const Lvl<double>& c,
+                  const AdjLvl& gc, cudaStream_t s);
+void adj_prolong(int dim, const Lvl<double>& f, const AdjLvl& gf, const Lvl<double>& c, const AdjLvl& gc, int diag,
                  cudaStream_t s);
 void adj_hierarchy2d(const Lvl<double>& a, const AdjLvl& g, int level, double sx, double sy, int nx0, double* dbx,
                      double* dby, double* dlam, cudaStream_t s);
+void adj_hier_xy2d(const Lvl<double>& a, const AdjLvl& g, int level, double cxy, int nx0, double* dxy,
+                   cudaStream_t s);
+void adj_hierarchy3d(const Lvl<double>& a, const AdjLvl& g, int level, const double* sq, int nx0, int ny0,
+                     const Lvl<double>* prev, double* const* gprev, const double* const* gcur, double* const* dbar,
+                     double* dlam, cudaStream_t s);
 int set_error_message(int code, const char* msg);
 
 namespace {
@@ -89,7 +98,7 @@ void find_segments(const JmgPlan* p, Tape& t) {
 // the forward schedule of one cycle (solver_2d.py:582-614), with the phi state each
 // operator reads (before) and writes (after) as snapshot indices
 void tape_cycle(const JmgPlan* p, Tape& t, std::vector<int>& cur, int lev, bool fcycle, bool skip_pre) {
-  const CycleParams cp = cycle_params(p, false);
+  const CycleParams cp = cycle_params(p, p->off_diag);
   auto sweep = [&]() {
     const int after = (int)t.snap_lev.size();
     t.snap_lev.push_back(lev);
@@ -123,9 +132,13 @@ Tape make_tape(const JmgPlan* p) {
   return t;
 }
 
+// adjoint arrays per level: pb, rb, T, gacc, the face gradients (2 or 3) and, with D_xy,
+// the four diagonal-coupling gradients
+int adj_arrays(const JmgPlan* p) { return 4 + p->dim + (p->off_diag ? 4 : 0); }
+
 struct AdjLayout {
   size_t total = 0;
-  std::vector<size_t> lvl;   // 6 arrays per level
+  std::vector<size_t> lvl;   // adj_arrays() arrays per level
   std::vector<size_t> snap;  // one level array per snapshot
   size_t ckpt = 0;           // (n + 1) level-0 arrays
   size_t zeros = 0;          // one level-0 array of zeros
@@ -143,7 +156,7 @@ AdjLayout adj_layout(const JmgPlan* p, const Tape& t) {
     off = align_up(off + b);
     return o;
   };
-  for (int l = 0; l < p->used; ++l) L.lvl.push_back(take(6 * p->lv[l].elems * 8));
+  for (int l = 0; l < p->used; ++l) L.lvl.push_back(take(adj_arrays(p) * p->lv[l].elems * 8));
   for (int lev : t.snap_lev) L.snap.push_back(take(p->lv[lev].elems * 8));
   L.ncyc = p->cfg.max_iters_outer > 0 ? (int)p->cfg.max_iters_outer : 0;
   L.ckpt = take((size_t)(L.ncyc + 1) * p->lv[0].elems * 8);
@@ -159,7 +172,26 @@ AdjLayout adj_layout(const JmgPlan* p, const Tape& t) {
 AdjLvl adj_lvl(const JmgPlan* p, void* aws, const AdjLayout& L, int l) {
   double* b = ptr<double>(aws, L.lvl[l]);
   const size_t n = p->lv[l].elems;
-  return AdjLvl{b, b + n, b + 2 * n, b + 3 * n, b + 4 * n, b + 5 * n};
+  AdjLvl g;
+  memset(&g, 0, sizeof(g));
+  g.pb = b;
+  g.rb = b + n;
+  g.T = b + 2 * n;
+  g.gacc = b + 3 * n;
+  g.gwx = b + 4 * n;
+  g.gwy = b + 5 * n;
+  double* q = b + 6 * n;
+  if (p->dim == 3) {
+    g.gwz = q;
+    q += n;
+  }
+  if (p->off_diag) {
+    g.gxll = q;
+    g.gxrl = q + n;
+    g.gxlr = q + 2 * n;
+    g.gxrr = q + 3 * n;
+  }
+  return g;
 }
 
 int fail(int code, const char* m) { return set_error_message(code, m); }
@@ -174,14 +206,14 @@ int fail(int code, const char* m) { return set_error_message(code, m); }
 // with snapshots, copy phi of the level after every sweep / prolongation
 void run_tape_forward(const JmgPlan* p, void* ws, void* aws, const AdjLayout& L, const Tape& t, bool snapshots,
                       cudaStream_t s) {
-  const CycleParams cp = cycle_params(p, false);
+  const CycleParams cp = cycle_params(p, p->off_diag);
   // current buffer of every level (one-pass sweeps swap a level's two buffers)
   std::vector<Lvl<double>> cur(p->used);
   for (int l = 0; l < p->used; ++l) cur[l] = lvl64(p, ws, l);
   size_t next_seg = 0;
   for (int k = 0; k < (int)t.ops.size(); ++k) {
     if (next_seg < t.segs.size() && t.segs[next_seg].first == k) {  // a single-block run
-      adj_seg_fwd(ptr<AdjTables>(aws, L.tabs), ptr<AdjSeg>(aws, L.segs) + next_seg, snapshots, cp.diag, s);
+      adj_seg_fwd(p->dim, ptr<AdjTables>(aws, L.tabs), ptr<AdjSeg>(aws, L.segs) + next_seg, snapshots, cp.diag, s);
       k = t.segs[next_seg].second;
       ++next_seg;
       continue;
@@ -207,7 +239,7 @@ void run_tape_forward(const JmgPlan* p, void* ws, void* aws, const AdjLayout& L,
 void adj_core(const JmgPlan* p, void* ws, void* aws, const AdjLayout& L, const Tape& tape, cudaStream_t s) {
   const size_t e0 = p->lv[0].elems;
   Lvl<double> l0 = lvl64(p, ws, 0);
-  const CycleParams cp = cycle_params(p, false);
+  const CycleParams cp = cycle_params(p, p->off_diag);
   const int nu1 = p->cfg.nu1 > 0 ? p->cfg.nu1 : 0;
   double* pre = ptr<double>(aws, L.pre);
   const double* zeros = ptr<double>(aws, L.zeros);
@@ -240,7 +272,7 @@ void adj_core(const JmgPlan* p, void* ws, void* aws, const AdjLayout& L, const T
     cudaMemcpyAsync(pre, l0.phi, e0 * 8, cudaMemcpyDeviceToDevice, s);
     Lvl<double> cur = l0;
     for (int k = 0; k < nu1; ++k) {
-      launch_sweep<double>(2, cur, s);
+      launch_sweep<double>(p->dim, cur, s);
       cudaMemcpyAsync(pre + (size_t)(k + 1) * e0, cur.phi, e0 * 8, cudaMemcpyDeviceToDevice, s);
     }
     if (cur.phi != l0.phi) cudaMemcpyAsync(l0.phi, cur.phi, e0 * 8, cudaMemcpyDeviceToDevice, s);
@@ -264,7 +296,7 @@ void adj_core(const JmgPlan* p, void* ws, void* aws, const AdjLayout& L, const T
     int seg = (int)tape.segs.size() - 1;
     for (int t = (int)tape.ops.size() - 1; t >= 0; --t) {
       if (seg >= 0 && tape.segs[seg].second == t) {  // a single-block run, in reverse
-        adj_seg_rev(ptr<AdjTables>(aws, L.tabs), ptr<AdjSeg>(aws, L.segs) + seg, cp.diag, s);
+        adj_seg_rev(p->dim, ptr<AdjTables>(aws, L.tabs), ptr<AdjSeg>(aws, L.segs) + seg, cp.diag, s);
         t = tape.segs[seg].first;
         --seg;
         continue;
@@ -272,16 +304,17 @@ void adj_core(const JmgPlan* p, void* ws, void* aws, const AdjLayout& L, const T
       const TapeOp& op = tape.ops[t];
       Lvl<double> a = lvl64(p, ws, op.lev);
       if (op.kind == OP_SWEEP) {
-        adj_sweep(a, g[op.lev], state(op.before), state(op.after), s);
+        adj_sweep(p->dim, a, g[op.lev], state(op.before), state(op.after), s);
       } else if (op.kind == OP_PROLONG) {
-        adj_prolong(a, g[op.lev], lvl64(p, ws, op.lev + 1), g[op.lev + 1], cp.diag, s);
+        adj_prolong(p->dim, a, g[op.lev], lvl64(p, ws, op.lev + 1), g[op.lev + 1], cp.diag, s);
       } else {
-        adj_restrict(a, g[op.lev], state(op.before), lvl64(p, ws, op.lev + 1), g[op.lev + 1], s);
+        adj_restrict(p->dim, a, g[op.lev], state(op.before), lvl64(p, ws, op.lev + 1), g[op.lev + 1], s);
       }
     }
   }
   if (p->cfg.skip_pre)
-    for (int k = nu1 - 1; k >= 0; --k) adj_sweep(l0, g[0], pre + (size_t)k * e0, pre + (size_t)(k + 1) * e0, s);
+    for (int k = nu1 - 1; k >= 0; --k)
+      adj_sweep(p->dim, l0, g[0], pre + (size_t)k * e0, pre + (size_t)(k + 1) * e0, s);
 }
 
 }  // namespace
@@ -296,21 +329,23 @@ size_t jmg_adjoint_workspace_bytes(const JmgPlan* p) {
   return adj_layout(p, make_tape(p)).total;
 }
 
-int jmg_solve_fixed_vjp(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs* c, const double* phi_bar,
-                        double* phi0_bar, double* rhs_bar, double* lam_bar, double* Dxx_bar, double* Dyy_bar,
-                        void* ws, size_t ws_bytes, void* aws, size_t aws_bytes, jmg_stream_t stream) {
+int jmg_solve_fixed_vjp_nd(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs* c,
+                           const double* phi_bar, double* phi0_bar, double* rhs_bar, double* lam_bar,
+                           double* const* D_bar, double* Dxy_bar, void* ws, size_t ws_bytes, void* aws,
+                           size_t aws_bytes, jmg_stream_t stream) {
   int rc = check_ws(p, ws, ws_bytes);
   if (rc) return rc;
-  if (p->dim != 2) return fail(JMG_ERR_VALUE, "the adjoint is implemented for 2D solves");
   if (!p->cfg.fixed) return fail(JMG_ERR_VALUE, "reverse mode needs fixed mode (as in the reference)");
   if (p->mixed) return fail(JMG_ERR_VALUE, "the adjoint differentiates the FP64 method (precision fp64)");
-  if (p->off_diag) return fail(JMG_ERR_VALUE, "the adjoint covers the 5-point stencil (no D_xy)");
   if (p->fcg) return fail(JMG_ERR_VALUE, "the adjoint differentiates the reference's iteration (outer richardson)");
   if ((rc = check_coeffs(p, c))) return rc;
-  if (!c->lam || !c->D[0] || !c->D[1])
-    return fail(JMG_ERR_VALUE, "the adjoint needs lambda, D_xx and D_yy as arrays (broadcast scalars first)");
-  if (!phi0 || !rhs || !phi_bar || !phi0_bar || !rhs_bar || !lam_bar || !Dxx_bar || !Dyy_bar)
-    return fail(JMG_ERR_VALUE, "NULL array argument");
+  const int dim = p->dim;
+  if (!c->lam || !D_bar) return fail(JMG_ERR_VALUE, "the adjoint needs lambda and D as arrays (broadcast scalars first)");
+  for (int a = 0; a < dim; ++a)
+    if (!c->D[a] || !D_bar[a])
+      return fail(JMG_ERR_VALUE, "the adjoint needs lambda and D as arrays (broadcast scalars first)");
+  if (p->off_diag && !Dxy_bar) return fail(JMG_ERR_VALUE, "a plan with D_xy needs the D_xy adjoint output");
+  if (!phi0 || !rhs || !phi_bar || !phi0_bar || !rhs_bar || !lam_bar) return fail(JMG_ERR_VALUE, "NULL array argument");
   const Tape tape = make_tape(p);
   const AdjLayout L = adj_layout(p, tape);
   if (!aws || aws_bytes < L.total || reinterpret_cast<uintptr_t>(aws) % kAlign)
@@ -357,14 +392,53 @@ int jmg_solve_fixed_vjp(JmgPlan* p, const double* phi0, const double* rhs, const
   launch_copy_out(b0, g0.pb, phi0_bar, s);
   launch_copy_out(b0, g0.rb, rhs_bar, s);
   JMG_ACUDA(cudaMemsetAsync(lam_bar, 0, dense * 8, s));
-  JMG_ACUDA(cudaMemsetAsync(Dxx_bar, 0, dense * 8, s));
-  JMG_ACUDA(cudaMemsetAsync(Dyy_bar, 0, dense * 8, s));
-  for (int l = 0; l < p->used; ++l) {
-    const double ix = p->grid.idel[0] * std::pow(0.5, l), iy = p->grid.idel[1] * std::pow(0.5, l);
-    adj_hierarchy2d(lvl64(p, ws, l), adj_lvl(p, aws, L, l), l, ix * ix, iy * iy, b0.nx, Dxx_bar, Dyy_bar, lam_bar, s);
+  for (int a = 0; a < dim; ++a) JMG_ACUDA(cudaMemsetAsync(D_bar[a], 0, dense * 8, s));
+  if (p->off_diag) JMG_ACUDA(cudaMemsetAsync(Dxy_bar, 0, dense * 8, s));
+  if (dim == 2) {
+    for (int l = 0; l < p->used; ++l) {
+      const double ix = p->grid.idel[0] * std::pow(0.5, l), iy = p->grid.idel[1] * std::pow(0.5, l);
+      const Lvl<double> a = lvl64(p, ws, l);
+      const AdjLvl g = adj_lvl(p, aws, L, l);
+      adj_hierarchy2d(a, g, l, ix * ix, iy * iy, b0.nx, D_bar[0], D_bar[1], lam_bar, s);
+      if (p->off_diag) adj_hier_xy2d(a, g, l, (ix * iy) * 0.25, b0.nx, Dxy_bar, s);
+    }
+  } else {
+    // the chained 3D hierarchy, coarsest level first. pb, rb and T of the levels >= 1 are
+    // free after the reverse sweep and hold the adjoints of their averaged D (zeroed here).
+    for (int l = 1; l < p->used; ++l) JMG_ACUDA(cudaMemsetAsync(adj_lvl(p, aws, L, l).pb, 0, 3 * p->lv[l].elems * 8, s));
+    for (int l = p->used - 1; l >= 0; --l) {
+      double sq[3];
+      for (int a = 0; a < 3; ++a) {
+        const double id = p->grid.idel[a] * std::pow(0.5, l);
+        sq[a] = id * id;
+      }
+      const AdjLvl g = adj_lvl(p, aws, L, l);
+      const double* gcur[3] = {g.T, g.pb, g.rb};
+      double* gprev[3] = {nullptr, nullptr, nullptr};
+      Lvl<double> prev;
+      if (l >= 2) {
+        const AdjLvl gp = adj_lvl(p, aws, L, l - 1);
+        gprev[0] = gp.T;
+        gprev[1] = gp.pb;
+        gprev[2] = gp.rb;
+        prev = lvl64(p, ws, l - 1);
+      }
+      adj_hierarchy3d(lvl64(p, ws, l), g, l, sq, b0.nx, b0.ny, l >= 2 ? &prev : nullptr, l >= 2 ? gprev : nullptr,
+                      l >= 1 ? gcur : nullptr, D_bar, lam_bar, s);
+    }
   }
   JMG_ACUDA(cudaGetLastError());
   return JMG_OK;
+}
+
+int jmg_solve_fixed_vjp(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs* c, const double* phi_bar,
+                        double* phi0_bar, double* rhs_bar, double* lam_bar, double* Dxx_bar, double* Dyy_bar,
+                        void* ws, size_t ws_bytes, void* aws, size_t aws_bytes, jmg_stream_t stream) {
+  if (p && p->dim != 2) return fail(JMG_ERR_VALUE, "jmg_solve_fixed_vjp is the 2D form (jmg_solve_fixed_vjp_nd: 3D)");
+  if (p && p->off_diag) return fail(JMG_ERR_VALUE, "jmg_solve_fixed_vjp has no D_xy output (jmg_solve_fixed_vjp_nd)");
+  double* D_bar[3] = {Dxx_bar, Dyy_bar, nullptr};
+  return jmg_solve_fixed_vjp_nd(p, phi0, rhs, c, phi_bar, phi0_bar, rhs_bar, lam_bar, D_bar, nullptr, ws, ws_bytes,
+                                aws, aws_bytes, stream);
 }
 
 }  // extern "C"

@@ -10,9 +10,12 @@
 namespace jmg {
 
 // adjoint arrays of one level: pb = adjoint of phi, rb = adjoint of rhs, T = scratch,
-// gacc / gwx / gwy = adjoints of A_cc and of the x / y face couplings
+// gacc / gwx / gwy / gwz = adjoints of A_cc and of the x / y / z face couplings (gwz in 3D),
+// gxll .. gxrr = adjoints of the diagonal couplings of the 9-point stencil (2D with D_xy);
+// absent arrays are nullptr
 struct AdjLvl {
-  double *pb, *rb, *T, *gacc, *gwx, *gwy;
+  double *pb, *rb, *T, *gacc, *gwx, *gwy, *gwz;
+  double *gxll, *gxrl, *gxlr, *gxrr;
 };
 
 enum { kAdjOpSweep = 0, kAdjOpRestrict = 1, kAdjOpProlong = 2 };
@@ -38,7 +41,7 @@ struct AdjTables {
 
 void adj_store_tables(const AdjTables& t, AdjTables* dst, cudaStream_t s);
 void adj_store_seg(const AdjSeg& g, AdjSeg* dst, cudaStream_t s);
-void adj_seg_fwd(const AdjTables* t, const AdjSeg* g, bool snapshots, int diag, cudaStream_t s);
-void adj_seg_rev(const AdjTables* t, const AdjSeg* g, int diag, cudaStream_t s);
+void adj_seg_fwd(int dim, const AdjTables* t, const AdjSeg* g, bool snapshots, int diag, cudaStream_t s);
+void adj_seg_rev(int dim, const AdjTables* t, const AdjSeg* g, int diag, cudaStream_t s);
 
 }  // namespace jmg
