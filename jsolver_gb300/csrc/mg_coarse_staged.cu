@@ -85,9 +85,10 @@ __device__ inline size_t level_elems(const Lvl<T>& a) {
 
 template <typename T, int DIM>
 __global__ void __launch_bounds__(512) k_coarse_staged(const LvlTable<T>* tab, CycleParams cp, int lev0, int fcycle,
-                                                      int skip_pre) {
+                                                      int skip_pre, CoarseOps ops) {
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ LvlTable<T> st;        // the levels, pointers into shared memory
+  __shared__ CoarseOps sops;        // the sub-cycle's operations
   __shared__ Lvl<T> top;            // the first coarse level in global memory
   __shared__ __align__(8) uint64_t bar;
   const int tid = threadIdx.x;
@@ -98,6 +99,7 @@ __global__ void __launch_bounds__(512) k_coarse_staged(const LvlTable<T>* tab, C
     int* dst = reinterpret_cast<int*>(&st);
     for (int k = tid; k < n; k += blockDim.x) dst[k] = src[k];
   }
+  stage_coarse_ops(ops, &sops);
   if (tid == 0) mbar_init(&bar, 1);
   __syncthreads();
   if (tid == 0) {
@@ -169,7 +171,8 @@ __global__ void __launch_bounds__(512) k_coarse_staged(const LvlTable<T>* tab, C
     mbar_wait(&bar, 0, kWaitPolls);
     return;
   }
-  blk_cycle<T, DIM>(&st, cp, lev0, fcycle != 0, skip_pre != 0);
+  if (sops.n > 0) blk_run<T, DIM>(&st, cp, &sops);
+  else blk_cycle<T, DIM>(&st, cp, lev0, fcycle != 0, skip_pre != 0);
   // phi of the first coarse level back to global memory (the frame is zero in both)
   {
     const size_t n = level_elems<T, DIM>(top);
@@ -202,10 +205,11 @@ int prepare_coarse_staged(int dim, size_t bytes) {
 template <typename T>
 void launch_coarse_staged(int dim, const LvlTable<T>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
                           size_t smem, int threads, cudaStream_t s) {
+  const CoarseOps ops = coarse_ops(cp, lev, fcycle != 0, skip_pre != 0);
   if (dim == 2)
-    launch_k(k_coarse_staged<T, 2>, dim3(1), dim3(threads), smem, s, tab, cp, lev, fcycle, skip_pre);
+    launch_k(k_coarse_staged<T, 2>, dim3(1), dim3(threads), smem, s, tab, cp, lev, fcycle, skip_pre, ops);
   else
-    launch_k(k_coarse_staged<T, 3>, dim3(1), dim3(threads), smem, s, tab, cp, lev, fcycle, skip_pre);
+    launch_k(k_coarse_staged<T, 3>, dim3(1), dim3(threads), smem, s, tab, cp, lev, fcycle, skip_pre, ops);
 }
 
 template int prepare_coarse_staged<float>(int, size_t);

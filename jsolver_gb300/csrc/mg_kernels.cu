@@ -122,17 +122,20 @@ __global__ void k_prolong3d(Lvl<T> f, Lvl<T> c, int bilinear) {
 // was an L2 round trip in front of the frame's first pass.
 template <typename T, int DIM>
 __global__ void __launch_bounds__(1024) k_coarse_cycle(const LvlTable<T>* tab, CycleParams cp, int lev, int fcycle,
-                                                      int skip_pre) {
+                                                      int skip_pre, CoarseOps ops) {
   pdl_enter();
   __shared__ LvlTable<T> stab;
+  __shared__ CoarseOps sops;
   {
     const int n = (int)(sizeof(LvlTable<T>) / sizeof(int));
     const int* src = reinterpret_cast<const int*>(tab);
     int* dst = reinterpret_cast<int*>(&stab);
     for (int k = threadIdx.x; k < n; k += blockDim.x) dst[k] = src[k];
   }
+  stage_coarse_ops(ops, &sops);
   __syncthreads();
-  blk_cycle<T, DIM>(&stab, cp, lev, fcycle != 0, skip_pre != 0);
+  if (sops.n > 0) blk_run<T, DIM>(&stab, cp, &sops);
+  else blk_cycle<T, DIM>(&stab, cp, lev, fcycle != 0, skip_pre != 0);
 }
 
 // FP32 2D coarse sub-cycle from shared memory. Every array of levels lev0 .. last (phi,
@@ -333,10 +336,11 @@ void launch_prolong(int dim, const Lvl<T>& f, const Lvl<T>& c, int diag, cudaStr
 template <typename T>
 void launch_coarse_cycle(int dim, const LvlTable<T>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
                          cudaStream_t s) {
+  const CoarseOps ops = coarse_ops(cp, lev, fcycle != 0, skip_pre != 0);
   if (dim == 2)
-    launch_k(k_coarse_cycle<T, 2>, dim3(1), dim3(1024), 0, s, tab, cp, lev, fcycle, skip_pre);
+    launch_k(k_coarse_cycle<T, 2>, dim3(1), dim3(1024), 0, s, tab, cp, lev, fcycle, skip_pre, ops);
   else
-    launch_k(k_coarse_cycle<T, 3>, dim3(1), dim3(1024), 0, s, tab, cp, lev, fcycle, skip_pre);
+    launch_k(k_coarse_cycle<T, 3>, dim3(1), dim3(1024), 0, s, tab, cp, lev, fcycle, skip_pre, ops);
 }
 
 template <typename T>

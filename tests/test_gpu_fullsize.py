@@ -31,7 +31,7 @@ from oracle import c_oracle, mg2d, mg3d  # noqa: E402
 
 TUNING = ("JMG_HOST_LOOP", "JMG_PDL", "JMG_COARSE_POINTS", "JMG_COARSE", "JMG_COARSE32", "JMG_FUSED", "JMG_FUSED2D",
           "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_RESTRICT3D", "JMG_PROLONG3D", "JMG_PROLONG2D", "JMG_FCG_BLOCKS",
-          "JMG_ADJ_BLOCK_POINTS")
+          "JMG_ADJ_BLOCK_POINTS", "JMG_COARSE_OPS", "JMG_FUSEDOPS", "JMG_FUSEDOPS_MAX", "JMG_COARSE_THREADS")
 
 
 def rel_l2(a, b):

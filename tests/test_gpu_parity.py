@@ -576,3 +576,42 @@ def test_staged_coarse_cycle_with_dxy(monkeypatch):
     np.testing.assert_array_equal(phi_s, phi_g)
     ref, _ = mg2d.solve_2d(g, g, *args, D_xy=dxy, fixed=True, max_iters_outer=4)
     assert rel_l2(phi_s, ref) < 1e-12
+
+
+OPS_CASES = [(2, 256, {}), (2, 256, {"gamma": 2}), (2, 256, {"fcycle": True}), (2, 128, {"fcycle": True, "gamma": 2}),
+             (2, 8, {"skip_pre": True}), (2, 128, {"nu1": 2, "nu2": 0}), (2, 128, {"nu1": 0, "nu2": 2}),
+             (2, 1024, {"precision": "mixed", "outer": "fcg", "inner_cycles": 2}), (3, 32, {"gamma": 2}),
+             (3, 64, {"precision": "mixed", "outer": "fcg", "fcycle": True})]
+
+
+@pytest.mark.parametrize("dim,m,form", OPS_CASES,
+                         ids=lambda x: ",".join(f"{k}={v}" for k, v in x.items()) if isinstance(x, dict) else str(x))
+@pytest.mark.parametrize("coarse", ["staged", "global"])
+def test_coarse_op_list_matches_recursion(dim, m, form, coarse, monkeypatch):
+    """The single-block coarse kernels walk a host-built list of the sub-cycle's operations;
+    JMG_COARSE_OPS=0 makes them walk the recursion instead. Same operations in the same
+    order, so the same bits and cycle counts, for every cycle shape and both kernels."""
+    g = grid_1D(m)
+    if dim == 2:
+        p = W.random_2d(m, seed=29)
+        grids, fn = (g, g), solve_2d
+        args = (p["phi0"], p["rhs"], p["lam"], p["D_xx"], p["D_yy"])
+    else:
+        p = W.random_3d(m, seed=29)
+        grids, fn = (g, g, g), solve_3d
+        args = (p["phi0"], p["rhs"], p["lam"], p["D_xx"], p["D_yy"], p["D_zz"])
+    kw = dict(form)
+    if kw.get("precision") == "mixed" or kw.get("outer") == "fcg":
+        kw.update(stop="residual", rtol=1e-9)
+    else:
+        kw.update(fixed=True, max_iters_outer=4)
+    if coarse == "global":
+        monkeypatch.setenv("JMG_COARSE", "global")
+    monkeypatch.setenv("JMG_COARSE_OPS", "0")
+    monkeypatch.setattr(_engine, "CACHE", _engine._Cache())
+    phi_r, c_r = fn(*grids, *args, **kw)
+    monkeypatch.delenv("JMG_COARSE_OPS")
+    monkeypatch.setattr(_engine, "CACHE", _engine._Cache())
+    phi_l, c_l = fn(*grids, *args, **kw)
+    assert int(c_r) == int(c_l)
+    np.testing.assert_array_equal(phi_l, phi_r)
