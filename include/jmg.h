@@ -43,7 +43,9 @@ enum {
   JMG_OK = 0,
   JMG_ERR_VALUE = 1,     /* invalid argument: the reference raises ValueError */
   JMG_ERR_CUDA = 2,      /* a CUDA runtime call failed */
-  JMG_ERR_WORKSPACE = 3  /* workspace missing or too small */
+  JMG_ERR_WORKSPACE = 3, /* workspace missing or too small */
+  JMG_ERR_TIMEOUT = 4    /* a bounded device-side wait ran out: the solve's result is void,
+                            the CUDA context stays usable (jmg_solve_check) */
 };
 
 enum { JMG_STOP_DISTANCE = 0, JMG_STOP_RESIDUAL = 1 };
@@ -245,6 +247,12 @@ int jmg_op_coarse_ws(JmgPlan* plan, int fp32, void* workspace, size_t workspace_
  * jmg_op_coarse_ws on a GPU; before that the single-block rule's choice). No reference
  * counterpart. */
 int jmg_plan_coarse_start(const JmgPlan* plan);
+/* First level of the 2D cycle that the persistent middle-level kernel takes (that level
+ * and every one below it in one cooperative launch, grid barriers between the fused
+ * operator pairs, the coarse sub-cycle on one of its blocks), or -1 when this plan's
+ * cycles run as separate launches. Valid after the plan's first solve. No reference
+ * counterpart: the middle and coarse branches of multigrid_cycle (solver_2d.py:582-614). */
+int jmg_plan_mid_start(const JmgPlan* plan);
 
 /* Whether this plan's solves run the fused operator pairs on a 2D level (fp32 != 0: the
  * FP32 cycles of a mixed plan): the last pre-sweep with the defect and restriction, the
@@ -267,6 +275,14 @@ int jmg_plan_sweep_launches(const JmgPlan* plan, int level, int fp32);
  * the part repeated per loop iteration (one cycle plus its stopping test). No reference
  * counterpart: it reports this library's launch schedule. */
 int jmg_plan_launch_counts(const JmgPlan* plan, int64_t* per_solve_fixed, int64_t* per_cycle);
+
+/* Waits for the stream and reports whether the last solve on this workspace completed its
+ * device-side waits: JMG_OK, or JMG_ERR_TIMEOUT when one ran out (a grid barrier of the
+ * persistent middle-level kernel, whose blocks wait on one another, or a staging copy of
+ * the coarse levels). Such a wait gives up after about a second, marks the iterate with
+ * NaN and ends the solve's loop, so a fault never hangs the device. No counterpart in the
+ * reference, whose XLA program has no device-side waits. */
+int jmg_solve_check(JmgPlan* plan, void* ws, size_t ws_bytes, jmg_stream_t stream);
 
 /* Relative residual ||rhs - L_h phi||_2 / ||rhs||_2 over interior indices 2..m, FP64,
  * written to the device double *out, for callers that cannot allocate device memory

@@ -221,6 +221,9 @@ def solve(grids, phi, rhs, lam, D, D_xy=None, guess=None, **opts):
                                          _stream_ptr(device)))
         if torch_in:
             return out, (int(cfg.max_iters_outer) if cfg.fixed else count)
+        # host inputs wait for the result anyway: confirm that no device-side wait ran out
+        _lib.check(_lib.load().jmg_solve_check(plan.handle, _ptr(ws), ctypes.c_size_t(ws.numel()),
+                                               _stream_ptr(device)))
         return out.cpu().numpy(), (int(cfg.max_iters_outer) if cfg.fixed else int(count.item()))
 
 

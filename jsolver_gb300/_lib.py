@@ -10,7 +10,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libjmg.so")
 
-JMG_OK, JMG_ERR_VALUE, JMG_ERR_CUDA, JMG_ERR_WORKSPACE = 0, 1, 2, 3
+JMG_OK, JMG_ERR_VALUE, JMG_ERR_CUDA, JMG_ERR_WORKSPACE, JMG_ERR_TIMEOUT = 0, 1, 2, 3, 4
 STOP_DISTANCE, STOP_RESIDUAL = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 OUTER_RICHARDSON, OUTER_FCG = 0, 1
@@ -68,9 +68,11 @@ _SIGS = {
     "jmg_op_smooth32_ws": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_size_t, _P]),
     "jmg_op_coarse_ws": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t, _P]),
     "jmg_plan_coarse_start": (ctypes.c_int, [_P]),
+    "jmg_plan_mid_start": (ctypes.c_int, [_P]),
     "jmg_plan_level_fused": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
     "jmg_op_smooth_restrict_ws": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_size_t, _P]),
     "jmg_plan_launch_counts": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
+    "jmg_solve_check": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "jmg_rel_residual_noalloc": (ctypes.c_int, [ctypes.POINTER(JmgGrid), _P, _P, ctypes.POINTER(JmgCoeffs), _P, _P]),
     "jmg_adjoint_workspace_bytes": (ctypes.c_size_t, [_P]),
     "jmg_tangent_workspace_bytes": (ctypes.c_size_t, [_P]),

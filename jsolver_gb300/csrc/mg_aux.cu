@@ -202,6 +202,8 @@ __global__ void k_loop_init(LoopState* st, const double* parts, int nparts, int 
   if (threadIdx.x != 0) return;
   st->count = 0;
   st->dist_bits = 0;
+  st->fault = 0;
+  st->bar_count = 0;
   int go = max_iters > 0;
   if (mode == 1) {
     st->res_norm = r;
@@ -230,6 +232,7 @@ __global__ void k_loop_step(LoopState* st, const double* parts, int nparts, int 
     st->rel_res = r / st->rhs_norm;
     go = go && (st->rel_res > rtol);
   }
+  if (st->fault) go = 0;  // a bounded wait ran out: the iterate is void, stop
   st->go = go;
   if (handle) cudaGraphSetConditional((cudaGraphConditionalHandle)handle, go ? 1u : 0u);
 }

@@ -85,6 +85,7 @@ int jmg_solve_batched(JmgPlan* p, int32_t batch, const double* phi0, const doubl
     if (cudaStreamWaitEvent(p->lane_streams[l], p->fork_event, 0) != cudaSuccess)
       return fail(JMG_ERR_CUDA, "cudaStreamWaitEvent failed");
   // problems in lane order; the first error stops issuing, the lanes are joined either way
+  p->in_batch = true;
   for (int b = 0; b < batch && rc == JMG_OK; ++b) {
     const int l = b % lanes;
     JmgCoeffs cb = *c;
@@ -94,6 +95,7 @@ int jmg_solve_batched(JmgPlan* p, int32_t batch, const double* phi0, const doubl
     rc = jmg_solve(p, phi0 + n * b, rhs + n * b, &cb, phi_out + n * b, counts_out ? counts_out + b : nullptr,
                    static_cast<char*>(ws) + lb * l, lb, p->lane_streams[l]);
   }
+  p->in_batch = false;
   for (int l = 0; l < lanes; ++l) {
     const bool ok = cudaEventRecord(p->lane_events[l], p->lane_streams[l]) == cudaSuccess &&
                     cudaStreamWaitEvent(s, p->lane_events[l], 0) == cudaSuccess;

@@ -238,6 +238,53 @@ int validate_and_layout(JmgPlan* p) {
 
 
 }  // namespace
+// The persistent middle-level kernel (mg_mid2d.cu), opt-in with JMG_MID=1, for 2D 5-point
+// plans with nu1, nu2 >= 1 whose coarse sub-cycle runs on the staged single block: it
+// takes over from the first level below level 0 with at most JMG_MID_POINTS padded points
+// (2^19 by default: 512^2 and smaller), provided every level from there to the coarse
+// block runs the fused operator pairs in the precision of the cycles (FP32 with mixed
+// precision, else FP64). JMG_MID_STALL=1 is the test mode whose first grid barrier never
+// completes. The operation list of the longest cycle form must fit kMaxMidOps, or the
+// kernel starts one level lower. Measured on GB300 it is slower than the separate
+// launches it replaces (2D 1024^2 mixed + FCG 9.6 against 6.3 ms; one launch 107 us
+// against about 49 us of launches per cycle): a grid-wide barrier costs more than a
+// kernel boundary with programmatic dependent launch, so it is not the default.
+static void mid_setup(JmgPlan* p) {
+  p->mid_start = -1;
+  p->mid_smem64 = p->mid_smem32 = 0;
+  p->mid_blocks = 0;
+  const char* me = getenv("JMG_MID");
+  const char* mp = getenv("JMG_MID_POINTS");
+  const char* ms = getenv("JMG_MID_STALL");
+  p->mid_stall = ms && ms[0] == '1';
+  const long long mid_max = (mp && atoll(mp) > 0) ? atoll(mp) : (1LL << 19);
+  const size_t staged = p->mixed ? p->coarse_staged32 : p->coarse_staged64;
+  if (!(me && me[0] == '1') || p->dim != 2 || p->off_diag || p->cluster_ranks || p->coarse_smem32 || !staged ||
+      p->cfg.nu1 < 1 || p->cfg.nu2 < 1 || p->coarse_start < 2)
+    return;
+  const CycleParams cp = cycle_params(p, false);
+  for (int l = 1; l < p->coarse_start; ++l) {
+    const LevelInfo& li = p->lv[l];
+    const long long pts = (long long)li.box.nx * li.box.ny;
+    if (pts > mid_max) continue;
+    bool fused = true;
+    for (int k = l; k < p->coarse_start; ++k) {
+      const LevelInfo& lk = p->lv[k];
+      fused = fused && lk.fuse_ops && (p->mixed ? lk.phi2_32 && !lk.onepass32 : lk.phi2 && !lk.onepass64);
+    }
+    if (!fused) continue;
+    MidOps ops;
+    if (!mid_ops(cp, p->coarse_start, l, p->cfg.fcycle != 0, true, &ops)) continue;
+    int blocks = 0;
+    const size_t smem = p->mixed ? prepare_mid2d<float>(staged, &blocks) : prepare_mid2d<double>(staged, &blocks);
+    if (!smem) return;
+    (p->mixed ? p->mid_smem32 : p->mid_smem64) = smem;
+    p->mid_blocks = blocks;
+    p->mid_start = l;
+    return;
+  }
+}
+
 // How the coarse levels of a cycle run. By default one block runs the levels of at most
 // 2048 points from global memory. With JMG_COARSE=cluster (and cluster support) a
 // thread-block cluster of 16 CTAs (8 where 16 is not allowed) takes every level from
@@ -310,6 +357,8 @@ int jmg::coarse_setup(JmgPlan* p) {
     if (b <= 200 * 1024 && prepare_coarse_smem32(b) == 0) p->coarse_smem32 = b;
   }
   prepare_fused_ops2d();  // kernel attributes, set outside any stream capture
+  if (p->dim == 3 && p->mixed) sweep_tma3d_ready();
+  mid_setup(p);
   cudaGetLastError();  // a refused attribute or occupancy query leaves no sticky error
   p->coarse_ready = true;
   return JMG_OK;
@@ -418,8 +467,21 @@ struct EmitTop {
 template <typename T>
 void emit_cycle(const JmgPlan* p, LvlTable<T>& tab, const LvlTable<T>* dtab, const CycleParams& cp, int lev,
                 bool fcycle, bool skip_pre, cudaStream_t s, long long* count = nullptr,
-                const EmitTop* top = nullptr, bool zero_phi = false) {
+                const EmitTop* top = nullptr, bool zero_phi = false, LoopState* st = nullptr) {
   const int dim = p->dim;
+  // 2D: this level and everything below it in one cooperative launch (mg_mid2d.cu)
+  const size_t mid_smem = sizeof(T) == 8 ? p->mid_smem64 : p->mid_smem32;
+  if (p->mid_now && lev == p->mid_start && mid_smem && !skip_pre && (count || st)) {
+    if (count) {
+      *count += 1;
+      return;
+    }
+    MidOps ops;
+    if (mid_ops(cp, p->coarse_start, lev, fcycle, zero_phi, &ops)) {
+      launch_mid2d<T>(dtab, st, cp, p->coarse_start, ops, mid_smem, p->mid_blocks, p->mid_stall, s);
+      return;
+    }
+  }
   // Fused operator pairs on a grid-wide 2D level (mg_fusedops2d.cu): the last pre-sweep
   // with the restriction, the prolongation with the first post-sweep; each writes the
   // level's second buffer and swaps, so a visit swaps twice.
@@ -470,11 +532,11 @@ void emit_cycle(const JmgPlan* p, LvlTable<T>& tab, const LvlTable<T>* dtab, con
   bool first = true;  // phi of level lev + 1 is zero until its first visit
   if (fcycle)
     for (int g = 0; g < cp.gamma; ++g) {
-      emit_cycle<T>(p, tab, dtab, cp, lev + 1, true, false, s, count, nullptr, first);
+      emit_cycle<T>(p, tab, dtab, cp, lev + 1, true, false, s, count, nullptr, first, st);
       first = false;
     }
   for (int g = 0; g < cp.gamma; ++g) {
-    emit_cycle<T>(p, tab, dtab, cp, lev + 1, false, false, s, count, nullptr, first);
+    emit_cycle<T>(p, tab, dtab, cp, lev + 1, false, false, s, count, nullptr, first, st);
     first = false;
   }
   if (count) *count += 1;
@@ -521,7 +583,7 @@ void emit_fcg_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaSt
       EmitTop top;
       top.zero_first = zero_first && k == 0;
       emit_cycle<float>(p, t32, ptr<LvlTable<float>>(ws, p->off_tab32), cp, 0, p->cfg.fcycle != 0, false, s,
-                        nullptr, &top);
+                        nullptr, &top, false, st);
     }
     launch_fcg32_iter(p->dim, l0, t32.l[0], t32.l[0].phi, ptr<float>(ws, p->off_d), ptr<float>(ws, p->off_q),
                       t32.l[0].rhs, fp, fp + 2 * np, fp + 4 * np, s);
@@ -534,7 +596,7 @@ void emit_fcg_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaSt
       EmitTop top;
       top.zero_first = zero_first && k == 0;
       emit_cycle<double>(p, tz, ptr<LvlTable<double>>(ws, p->off_tab64z), cp, 0, p->cfg.fcycle != 0, false, s,
-                         nullptr, &top);
+                         nullptr, &top, false, st);
     }
     launch_fcg_iter<double>(p->dim, l0, tz.l[0].phi, ptr<double>(ws, p->off_d), ptr<double>(ws, p->off_q),
                             ptr<double>(ws, p->off_rho), nullptr, fp, fp + 2 * np, fp + 4 * np, s);
@@ -558,7 +620,7 @@ void emit_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaStream
   if (!p->mixed) {
     LvlTable<double> tab = make_table<double>(p, ws);
     emit_cycle<double>(p, tab, ptr<LvlTable<double>>(ws, p->off_tab64), cp, 0, p->cfg.fcycle != 0,
-                       p->cfg.skip_pre != 0, s);
+                       p->cfg.skip_pre != 0, s, nullptr, nullptr, false, st);
   } else if (mixed_fused(p)) {
     // FP64 iterative refinement around FP32 cycles. r32 = float(rhs - L_h phi) is already
     // in place (prologue or previous step). FP32 cycles solve L_h e = r from e = 0; the
@@ -570,7 +632,7 @@ void emit_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaStream
       EmitTop top;
       top.zero_first = k == 0;
       emit_cycle<float>(p, t32, ptr<LvlTable<float>>(ws, p->off_tab32), cp, 0, p->cfg.fcycle != 0, false, s,
-                        nullptr, &top);
+                        nullptr, &top, false, st);
     }
     launch_add_correction(p->dim, l0, t32.l[0].phi, s);
     launch_residual_f32_2d(l0, t32.l[0].rhs, parts, s);
@@ -584,7 +646,8 @@ void emit_body(const JmgPlan* p, void* ws, unsigned long long handle, cudaStream
     launch_zero_f32(p->lv[0].box, t32.l[0].phi, s);
     const int inner = p->cfg.inner_cycles > 0 ? p->cfg.inner_cycles : 1;
     for (int k = 0; k < inner; ++k)
-      emit_cycle<float>(p, t32, ptr<LvlTable<float>>(ws, p->off_tab32), cp, 0, p->cfg.fcycle != 0, false, s);
+      emit_cycle<float>(p, t32, ptr<LvlTable<float>>(ws, p->off_tab32), cp, 0, p->cfg.fcycle != 0, false, s,
+                        nullptr, nullptr, false, st);
     launch_add_correction(p->dim, l0, t32.l[0].phi, s);
     if (mixed_resid(p)) launch_residual_partials<double>(p->dim, l0, l0.phi, parts, p->nparts, s, t32.l[0].rhs);
   }
@@ -655,9 +718,9 @@ long long body_launches(const JmgPlan* p) {
   return n;
 }
 
-int build_graph(JmgPlan* p, void* ws, cudaGraphExec_t* out) {
+int capture_graph(JmgPlan* p, void* ws, cudaGraphExec_t* out) {
   for (const JmgPlan::GraphSlot& g : p->graphs)
-    if (g.ws == ws) {
+    if (g.ws == ws && g.mid == p->mid_now) {
       *out = g.exec;
       return JMG_OK;
     }
@@ -695,9 +758,28 @@ int build_graph(JmgPlan* p, void* ws, cudaGraphExec_t* out) {
   cudaGraphExec_t exec;
   JMG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
   cudaGraphDestroy(graph);
-  p->graphs.push_back({ws, exec});
+  p->graphs.push_back({ws, exec, p->mid_now});
   *out = exec;
   return JMG_OK;
+}
+
+// The loop graph; if capturing or instantiating it with the cooperative middle-level
+// kernel fails (a runtime that does not take cooperative kernel nodes in conditional
+// graphs), the plan drops that kernel and captures the plain launches instead.
+int build_graph(JmgPlan* p, void* ws, cudaGraphExec_t* out) {
+  const int rc = capture_graph(p, ws, out);
+  if (rc == JMG_OK || !p->mid_now) return rc;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (p->cap && cudaStreamIsCapturing(p->cap, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(p->cap, &g);
+    if (g) cudaGraphDestroy(g);
+  }
+  cudaGetLastError();
+  p->mid_start = -1;
+  p->mid_smem32 = p->mid_smem64 = 0;
+  p->mid_now = false;
+  return capture_graph(p, ws, out);
 }
 
 HierInputs hier_inputs(const JmgPlan* p, const JmgCoeffs* c) {
@@ -941,8 +1023,11 @@ int jmg_solve(JmgPlan* p, const double* phi0, const double* rhs, const JmgCoeffs
     for (int k = 0; k < nu1; ++k) launch_sweep<double>(p->dim, cur, s);
     launch_distance_snapshot(b0, phi_old, l0.phi, st, s);  // phi_old <- smoothed phi
   }
-  // 4. the loop
+  // 4. the loop (the cooperative middle-level kernel only outside the lanes of a batch)
+  p->mid_now = p->mid_start >= 0 && !p->in_batch;
   const bool runs = p->cfg.max_iters_outer > 0;
+  // the loop's prologue clears the fault flag jmg_solve_check reads; without a loop, here
+  if (!runs) JMG_CUDA(cudaMemsetAsync(&st->fault, 0, sizeof(int), s));
   if (runs && !p->host_loop) {
     cudaGraphExec_t exec = nullptr;
     if ((rc = build_graph(p, ws, &exec))) return rc;
@@ -1163,6 +1248,7 @@ int jmg_op_coarse_ws(JmgPlan* p, int fp32, void* ws, size_t bytes, jmg_stream_t 
 }
 
 int jmg_plan_coarse_start(const JmgPlan* p) { return p ? p->coarse_start : -1; }
+int jmg_plan_mid_start(const JmgPlan* p) { return p && p->mid_start >= 0 && p->mid_now ? p->mid_start : -1; }
 
 int jmg_plan_level_fused(const JmgPlan* p, int level, int fp32) {
   if (!p || level < 0 || level + 1 >= p->used) return 0;
@@ -1201,6 +1287,31 @@ int jmg_plan_sweep_launches(const JmgPlan* p, int level, int fp32) {
   const LevelInfo& li = p->lv[level];
   if (fp32 ? li.onepass32 : li.onepass64) return 1;
   return p->off_diag ? 4 : 2;
+}
+
+int jmg_solve_check(JmgPlan* p, void* ws, size_t bytes, jmg_stream_t stream) {
+  int rc = check_ws(p, ws, bytes);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  // the loop state's flag (grid barriers) and the level tables' flags (staging copies)
+  int flags[4] = {0, 0, 0, 0};
+  JMG_CUDA(cudaMemcpyAsync(&flags[0], &ptr<LoopState>(ws, p->off_state)->fault, sizeof(int), cudaMemcpyDeviceToHost, s));
+  JMG_CUDA(cudaMemcpyAsync(&flags[1], &ptr<LvlTable<double>>(ws, p->off_tab64)->fault, sizeof(int),
+                           cudaMemcpyDeviceToHost, s));
+  if (p->mixed)
+    JMG_CUDA(cudaMemcpyAsync(&flags[2], &ptr<LvlTable<float>>(ws, p->off_tab32)->fault, sizeof(int),
+                             cudaMemcpyDeviceToHost, s));
+  if (p->fcg && !p->mixed)
+    JMG_CUDA(cudaMemcpyAsync(&flags[3], &ptr<LvlTable<double>>(ws, p->off_tab64z)->fault, sizeof(int),
+                             cudaMemcpyDeviceToHost, s));
+  JMG_CUDA(cudaStreamSynchronize(s));
+  const int tma = p->dim == 3 && p->mixed ? sweep_tma3d_fault() : 0;
+  if (flags[0] || flags[1] || flags[2] || flags[3] || tma)
+    return set_err(JMG_ERR_TIMEOUT,
+                   "a bounded device-side wait of the last solve on this workspace ran out (%s); its result is void",
+                   flags[0] ? "a grid barrier of the middle-level kernel"
+                            : tma ? "a plane copy of the one-pass 3D sweep" : "a staging copy of the coarse levels");
+  return JMG_OK;
 }
 
 const char* jmg_last_error(void) { return g_last_error.c_str(); }

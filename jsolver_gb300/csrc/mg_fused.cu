@@ -187,6 +187,9 @@ int fused_wave_permille(int mx, int my, int mz) {
 
 template <typename T>
 void launch_sweep_fused3d(Lvl<T>& a, bool zero_in, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (sweep_tma3d_enabled() && launch_sweep_tma3d(a, zero_in, s)) return;
+  }
   const int kchunk = fused_chunk3d(a.mx, a.my, a.mz, kBlocksPerSMT<T>);
   dim3 g((a.mx - 1 + kTX - 1) / kTX, (a.my - 1 + kTY - 1) / kTY, (a.mz - 1 + kchunk - 1) / kchunk);
   launch_k(k_sweep_fused3d<T>, g, dim3(kThreads), 0, s, a, a.phi2, zero_in ? 1 : 0, kchunk);

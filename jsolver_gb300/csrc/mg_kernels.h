@@ -39,7 +39,10 @@ struct LoopState {
   double rhs_norm;               // ||rhs||_2 over the interior (residual stop)
   double rel_res;                // res_norm / rhs_norm
   int go;                        // last loop decision
-  int pad;
+  int fault;                     // a bounded device-side wait ran out (the loop then ends)
+  unsigned bar_count;            // grid barrier of the persistent middle-level kernel
+                                 // (mg_mid2d.cu): arrivals, and the generation on a line
+  alignas(128) unsigned bar_gen; // of its own, so that polling it does not slow the adds
 };
 
 // one full sweep (two colour passes, in place); with zero_init it starts from phi = 0
@@ -47,6 +50,13 @@ template <typename T> void launch_sweep(int dim, Lvl<T>& a, cudaStream_t s, bool
 // One-pass red-black sweep of a 3D level from a.phi into a.phi2, then the two pointers
 // swap (mg_fused.cu); bit-identical to launch_sweep. zero_in: phi is taken as zero.
 template <typename T> void launch_sweep_fused3d(Lvl<T>& a, bool zero_in, cudaStream_t s);
+// mg_sweep_tma3d.cu: the same sweep for FP32 levels with its plane tiles fed by TMA copies
+// (opt-in, JMG_SWEEP3D=tma). false: it cannot run here (no tensor-map encoder or not
+// enough shared memory), nothing was launched.
+bool sweep_tma3d_ready();
+bool sweep_tma3d_enabled();
+bool launch_sweep_tma3d(Lvl<float>& a, bool zero_in, cudaStream_t s);
+int sweep_tma3d_fault();  // reads and clears the flag of a sweep whose copies did not arrive
 // The 2D one-pass sweep (tiles of 64 x 16 with a halo, mg_fused.cu), and the dispatch of
 // either by dimension; levels with a second phi buffer only, no D_xy.
 template <typename T> void launch_sweep_onepass2d(Lvl<T>& a, bool zero_in, cudaStream_t s);
@@ -116,6 +126,27 @@ template <typename T> int prepare_coarse_staged(int dim, size_t bytes);
 template <typename T>
 void launch_coarse_staged(int dim, const LvlTable<T>* tab, const CycleParams& cp, int lev, int fcycle, int skip_pre,
                           size_t smem, int threads, cudaStream_t s);
+// mg_mid2d.cu: the 2D middle levels (fused operator pairs between grid barriers) and the
+// coarse sub-cycle (block 0, levels staged in shared memory) in one cooperative launch.
+// Operation list: (kind << 12) | (flag << 8) | level, in the order of the recursion; flag
+// is zero_in for kMidSR and the colour for kMidColor.
+constexpr int kMaxMidOps = 4000;
+struct MidOps {
+  int n;
+  unsigned short op[kMaxMidOps];
+};
+enum { kMidBlkSweep = 0, kMidBlkRestrict = 1, kMidBlkProlong = 2, kMidSR = 3, kMidPS = 4, kMidColor = 5 };
+// the list of multigrid_cycle(lev) for levels lev .. coarse_start - 1 fused and the coarse
+// levels on block 0; false when it exceeds kMaxMidOps
+bool mid_ops(const CycleParams& cp, int coarse_start, int lev, bool fcycle, bool zero_phi, MidOps* out);
+// sets the kernel's attributes; returns its dynamic shared-memory bytes (0: it cannot run:
+// no cooperative launch, or one block with this much shared memory does not fit an SM)
+// and the grid size (one block per SM)
+template <typename T> size_t prepare_mid2d(size_t staged_bytes, int* blocks);
+// stall: test mode whose first grid barrier never completes (its bounded wait runs out)
+template <typename T>
+cudaError_t launch_mid2d(const LvlTable<T>* tab, LoopState* st, const CycleParams& cp, int coarse_start,
+                         const MidOps& ops, size_t smem, int blocks, bool stall, cudaStream_t s);
 // copies a level table into device memory (the coarse kernel reads it from there)
 template <typename T> void launch_store_table(const LvlTable<T>& tab, LvlTable<T>* dst, cudaStream_t s);
 

@@ -50,6 +50,7 @@ struct JmgPlan {
   struct GraphSlot {
     void* ws;
     cudaGraphExec_t exec;
+    bool mid;  // captured with the persistent middle-level kernel
   };
   // more than the 32 lanes of a batched solve, so that a full batch alternating with
   // single solves on other workspaces keeps every lane's graph
@@ -86,6 +87,18 @@ struct JmgPlan {
   // FP32 tables (0: the global-memory kernel instead) and the block size
   size_t coarse_staged64 = 0, coarse_staged32 = 0;
   int coarse_threads = 512;
+  // 2D: the levels from mid_start down (fused operator pairs) and the coarse sub-cycle in
+  // one cooperative launch (mg_mid2d.cu); mid_start -1: not used. Dynamic shared memory of
+  // the FP64 and FP32 kernels (0: that precision does not use it), grid size, and the test
+  // mode whose first barrier never completes (JMG_MID_STALL=1)
+  int mid_start = -1;
+  size_t mid_smem64 = 0, mid_smem32 = 0;
+  int mid_blocks = 0;
+  bool mid_stall = false;
+  // whether the cycle being emitted may use it: not in the lanes of a batched solve, whose
+  // concurrent cooperative launches would compete for the same SMs
+  bool mid_now = false;
+  bool in_batch = false;  // jmg_solve_batched is issuing its lanes' solves
 };
 
 

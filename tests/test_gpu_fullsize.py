@@ -97,6 +97,19 @@ def test_3d_256_onepass_fp32_sweep_bit_identical(p3d, monkeypatch):
     np.testing.assert_array_equal(phi_a, phi_b)
 
 
+def test_3d_256_tma_sweep_equals_register_sweep(p3d, monkeypatch):
+    """The same mixed solve with the level-0 one-pass sweep fed by register loads (the
+    default) and by TMA copies (JMG_SWEEP3D=tma): the same bits."""
+    grids, args, _ = p3d
+    kw = dict(precision="mixed", fixed=True, max_iters_outer=3, fcycle=True)
+    monkeypatch.setattr(_engine, "CACHE", _engine._Cache())
+    phi_a, _ = solve_3d(*grids, *args, **kw)
+    monkeypatch.setenv("JMG_SWEEP3D", "tma")
+    monkeypatch.setattr(_engine, "CACHE", _engine._Cache())
+    phi_b, _ = solve_3d(*grids, *args, **kw)
+    np.testing.assert_array_equal(phi_a, phi_b)
+
+
 def test_2d_1024_headline_form_reaches_rtol(p2d):
     grids, args, p = p2d
     phi, c = solve_2d(*grids, *args, stop="residual", rtol=1e-10, precision="mixed", outer="fcg", inner_cycles=2)
