@@ -593,12 +593,16 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
                                stream, flush, 20) / per
         n0 = (m + 3) ** dim
         alg_sweep = (dim + 4) * elem * n0  # (d+4)*s*N0: phi, rhs, d faces, 1/A_cc read; phi written
+        # the one-pass FP32 3D sweep is k_sweep_tma3d (TMA plane copies) unless JMG_SWEEP3D=regs
+        tma = dim == 3 and fp32 and launches_per_sweep == 1 and os.environ.get("JMG_SWEEP3D") != "regs"
         traffic = load_json("profiles/traffic.json").get(
-            f"sweep_{'fp32' if fp32 else 'fp64'}_{dim}d_{m}" + ("_onepass" if launches_per_sweep == 1 else ""))
+            f"sweep_{'fp32' if fp32 else 'fp64'}_{dim}d_{m}" +
+            ("_tma" if tma else "_onepass" if launches_per_sweep == 1 else ""))
         peaks = load_json("MEASURED_PEAKS.json")
         peak = float(peaks.get("hbm_gbs", 6800.0))
         peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-        sweep_kernel = (f"{'k_sweep_fused3d' if dim == 3 else 'k_sweep_onepass2d'}<{'float' if fp32 else 'double'}> "
+        sweep_kernel = (f"{('k_sweep_tma3d' if tma else 'k_sweep_fused3d') if dim == 3 else 'k_sweep_onepass2d'}"
+                        f"<{'float' if fp32 else 'double'}> "
                         "(fine level; one launch per sweep)" if launches_per_sweep == 1 else
                         f"k_sweep_color{dim}d<{'float' if fp32 else 'double'}> (fine level; "
                         f"{launches_per_sweep} launches per sweep)")

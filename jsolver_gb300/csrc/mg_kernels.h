@@ -51,8 +51,8 @@ template <typename T> void launch_sweep(int dim, Lvl<T>& a, cudaStream_t s, bool
 // swap (mg_fused.cu); bit-identical to launch_sweep. zero_in: phi is taken as zero.
 template <typename T> void launch_sweep_fused3d(Lvl<T>& a, bool zero_in, cudaStream_t s);
 // mg_sweep_tma3d.cu: the same sweep for FP32 levels with its plane tiles fed by TMA copies
-// (opt-in, JMG_SWEEP3D=tma). false: it cannot run here (no tensor-map encoder or not
-// enough shared memory), nothing was launched.
+// (the default; JMG_SWEEP3D=regs keeps k_sweep_fused3d). false: it cannot run here (no
+// tensor-map encoder or not enough shared memory), nothing was launched.
 bool sweep_tma3d_ready();
 bool sweep_tma3d_enabled();
 bool launch_sweep_tma3d(Lvl<float>& a, bool zero_in, cudaStream_t s);

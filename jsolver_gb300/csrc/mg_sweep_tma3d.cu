@@ -39,23 +39,34 @@ namespace jmg {
 
 namespace {
 
-constexpr int kTX = 64, kTY = 8;           // interior points of a tile (x, y)
-constexpr int kBX = kTX + 4, kBY = kTY + 4; // box: x from i0-2, y from j0-2
-constexpr int kBoxBytes = kBX * kBY * 4;    // 3264
-constexpr int kSlotElems = 832;             // 3328 bytes: boxes start on 128-byte boundaries
-constexpr int kArrays = 6;                  // phi, rhs, wx, wy, wz, invd
-enum { A_PHI = 0, A_RHS = 1, A_WX = 2, A_WY = 3, A_WZ = 4, A_INVD = 5 };
-constexpr int kSlots = 8;                   // plane ring
-constexpr int kAhead = 3;                   // planes in flight beyond the step's window
-constexpr int kRX = kTX + 2, kRY = kTY + 2; // red ring region
-constexpr int kRed = kRX * kRY / 2;         // 330 red points per plane
-constexpr int kBlack = 256;                // black role: 8 warps, two points per thread
-constexpr int kThreads = 640;               // + 330 red-role threads (11 warps) and spare lanes
+constexpr int kTX = 64, kTY = 8;  // interior points of a tile (x, y)
+constexpr int kBX = kTX + 4;      // box width: x from i0-2 (a 16-byte aligned start)
+// Boxes (rows; y from j0-2 for 12 and 11 rows, from j0-1 for 10): phi 12 (the red ring's
+// neighbours), wy 11 (couplings to the row below the ring), wz, wx, rhs, 1/A_cc 10 (the
+// ring's rows). Sub-box sizes are rounded up to 128 bytes.
+enum { M_PHI = 0, M_WZ = 1, M_WX = 2, M_WY = 3, M_RHS = 4, M_INVD = 5, kMaps = 6 };
+constexpr int kRowsPhi = 12, kRowsWy = 11, kRows10 = 10;
+constexpr int kRows[kMaps] = {kRowsPhi, kRows10, kRows10, kRowsWy, kRows10, kRows10};
+constexpr int kPhiE = 832, kWzE = 704;               // floats of the (phi, wz) sub-boxes
+constexpr int kWxE = 704, kWyE = 768, kRhsE = 704, kInvE = 704;
+constexpr int kAE = kPhiE + kWzE;                    // group A slot: phi, wz (1536 floats)
+constexpr int kBE = kWxE + kWyE + kRhsE + kInvE;     // group B slot: wx, wy, rhs, invd (2880)
+// Plane ring: step k issues group A of plane k+kDA and group B of plane k+kDB; group A of
+// plane q is read until step q-1 and group B until step q-2, so kDA slots and kDB-1 slots
+// suffice. The copies have kDA-4 and kDB-3 steps of lead beyond the step that waits for
+// them.
+constexpr int kDA = 4, kDB = 4;
+constexpr int kASlots = kDA, kBSlots = kDB - 1;
+constexpr int kRX = kTX + 2, kRY = kTY + 2;          // red ring region
+constexpr int kRed = kRX * kRY / 2;                  // 330 red points per plane
+constexpr int kThreads = 384;                        // black: t < 256; red: t < 330
+constexpr int kBlocksPerSM = 3;
 constexpr int kRedSlots = 4;
-constexpr size_t kSmem = (size_t)kSlots * kArrays * kSlotElems * 4;  // 159,744 bytes
+constexpr size_t kSmem = (size_t)(kASlots * kAE + kBSlots * kBE) * 4;  // 59,136 bytes
+constexpr uint32_t kBytesPhi = kBX * kRowsPhi * 4, kBytesWy = kBX * kRowsWy * 4, kBytes10 = kBX * kRows10 * 4;
 
 struct Maps {
-  CUtensorMap m[kArrays];
+  CUtensorMap m[kMaps];
 };
 
 __device__ __forceinline__ void tma_plane(const CUtensorMap* map, float* dst, int x, int y, int z, uint64_t* bar) {
@@ -69,12 +80,23 @@ __device__ __forceinline__ void tma_plane(const CUtensorMap* map, float* dst, in
 // set by a block whose wait for its copies ran out (read and cleared by jmg_solve_check)
 __device__ int g_tma_fault;
 
-__global__ void __launch_bounds__(kThreads, 1)
+// Step k of a tile's march (k from ka-3 to kb-1):
+//   thread 0 issues the copies of group A of plane k+kDA and group B of plane k+kDB (into
+//   the slots planes k and k+1 left);
+//   the red threads compute red(k+2) from phi(k+1 .. k+3), wz(k+1 .. k+2) and the group-B
+//   arrays of plane k+2;
+//   the black threads (k >= ka) update black(k) from the red values in shared memory and
+//   coefficients read through L2 a step ahead (their copies passed through it earlier);
+//   thread 0 waits for the next step's copies; one barrier.
+// Steps ka-3 .. ka-1 only produce red(ka-1), red(ka), red(ka+1).
+__global__ void __launch_bounds__(kThreads, kBlocksPerSM)
     k_sweep_tma3d(const __grid_constant__ Maps maps, Lvl<float> a, float* __restrict__ out, int zero_in,
                   int per_block) {
-  extern __shared__ __align__(1024) float ring[];  // [slot][array][12][68] (832-float pitch)
+  extern __shared__ __align__(1024) float sm[];  // [4][A slot] then [3][B slot]
+  float* const sA = sm;
+  float* const sB = sm + kASlots * kAE;
   __shared__ float red[kRedSlots][kRY][kRX];
-  __shared__ __align__(8) uint64_t bar[kSlots];
+  __shared__ __align__(8) uint64_t barA[kASlots], barB[kBSlots];
   const int tid = threadIdx.x;
   const int planes = a.mz - 1;  // interior planes 2 .. mz
   const int ntx = (a.mx - 1 + kTX - 1) / kTX, nty = (a.my - 1 + kTY - 1) / kTY;
@@ -82,139 +104,166 @@ __global__ void __launch_bounds__(kThreads, 1)
   long long g = (long long)blockIdx.x * per_block;
   const long long g1 = g + per_block < total ? g + per_block : total;
   const bool zin = zero_in != 0;
-  const int first = zin ? 1 : 0;  // phi is not copied from a zero initial guess
-  const uint32_t bytes = (uint32_t)((kArrays - first) * kBoxBytes);
+  const uint32_t bytesA = (zin ? 0u : kBytesPhi) + kBytes10;
+  const uint32_t bytesB = 3 * kBytes10 + kBytesWy;
   const int P = a.P, S = (int)a.S;
   const int par = first_color_parity<3>();
-  if (tid == 0)
-    for (int s = 0; s < kSlots; ++s) mbar_init(&bar[s], 1);
+  if (tid == 0) {
+    for (int s = 0; s < kASlots; ++s) mbar_init(&barA[s], 1);
+    for (int s = 0; s < kBSlots; ++s) mbar_init(&barB[s], 1);
+  }
   pdl_enter();
   __syncthreads();
-  unsigned seq = 0;     // planes of the finished segments (slot = seq % 8, phase = seq / 8)
-  unsigned issued = 0;  // thread 0: planes issued so far
+  unsigned seqA = 0, seqB = 0;        // copies of the finished segments, per group
+  unsigned issuedA = 0, issuedB = 0;  // thread 0: copies issued so far
   bool ok = true;
-  // Roles in separate warps, so that a step's black and red updates run side by side:
-  // black, warps 0-7: tile row ty, columns 2tx, 2tx+1 (thread 0 also issues the copies);
-  // red, threads 256 .. 585: one point of the ring region per plane (row rr, pair rx).
-  const bool blk_role = tid < kBlack;
+  const bool red_role = tid < kRed;
+  const int rr = red_role ? tid / (kRX / 2) : 0;
+  const int rx = red_role ? 2 * (tid - rr * (kRX / 2)) : 0;
+  const bool blk_role = tid < 256;
   const int tx = tid & 31, ty = tid >> 5;
-  const int rt = tid - kBlack;
-  const bool red_role = rt >= 0 && rt < kRed;
-  const int rr = red_role ? rt / (kRX / 2) : 0;
-  const int rx = red_role ? 2 * (rt - rr * (kRX / 2)) : 0;
   while (g < g1 && ok) {
     const int tile = (int)(g / planes);
     const int ka = 2 + (int)(g - (long long)tile * planes);
     const long long tend = (long long)(tile + 1) * planes;
     const int kb = 2 + (int)((g1 < tend ? g1 : tend) - (long long)tile * planes);  // planes ka .. kb-1
     const int i0 = 2 + kTX * (tile % ntx), j0 = 2 + kTY * (tile / ntx);
-    const unsigned base = seq - (unsigned)(ka - 2);  // sequence number of plane q: base + q
-    const int last_issue = kb + 1;                   // red(kb) reads phi(kb + 1)
-    seq = base + (unsigned)last_issue + 1u;
-    if (tid == 0)
-      for (int q = ka - 2; q <= ka + kSlots - 3 && q <= last_issue; ++q) {
-        const unsigned sl = (base + (unsigned)q) & (kSlots - 1);
-        mbar_expect_tx(&bar[sl], bytes);
-        for (int arr = first; arr < kArrays; ++arr)
-          tma_plane(&maps.m[arr], ring + (sl * kArrays + arr) * kSlotElems, i0 - 2, j0 - 2, q, &bar[sl]);
-        ++issued;
-      }
-    auto plane = [&](int q) -> const float* { return ring + ((base + (unsigned)q) & (kSlots - 1)) * (kArrays * kSlotElems); };
-    auto wait = [&](int q) {
-      const unsigned n = base + (unsigned)q;
-      return mbar_wait(&bar[n & (kSlots - 1)], (n >> 3) & 1u, kWaitPolls);
+    // sequence numbers: group A plane q -> baseA + q (planes ka-2 .. kb+1), group B plane
+    // q -> baseB + q (planes ka-1 .. kb)
+    const unsigned baseA = seqA - (unsigned)(ka - 2), baseB = seqB - (unsigned)(ka - 1);
+    const int lastA = kb + 1, lastB = kb;
+    seqA = baseA + (unsigned)lastA + 1u;
+    seqB = baseB + (unsigned)lastB + 1u;
+    auto slotA = [&](int q) { return (baseA + (unsigned)q) % kASlots; };
+    auto slotB = [&](int q) { return (baseB + (unsigned)q) % kBSlots; };
+    auto issueA = [&](int q) {
+      const unsigned s = slotA(q);
+      float* d = sA + s * kAE;
+      mbar_expect_tx(&barA[s], bytesA);
+      if (!zin) tma_plane(&maps.m[M_PHI], d, i0 - 2, j0 - 2, q, &barA[s]);
+      tma_plane(&maps.m[M_WZ], d + kPhiE, i0 - 2, j0 - 1, q, &barA[s]);
+      ++issuedA;
     };
-    // red role: its ring point's box element for column offset 0, and whether the row is
-    // interior; the red one of the pair alternates with the plane
+    auto issueB = [&](int q) {
+      const unsigned s = slotB(q);
+      float* d = sB + s * kBE;
+      mbar_expect_tx(&barB[s], bytesB);
+      tma_plane(&maps.m[M_WX], d, i0 - 2, j0 - 1, q, &barB[s]);
+      tma_plane(&maps.m[M_WY], d + kWxE, i0 - 2, j0 - 2, q, &barB[s]);
+      tma_plane(&maps.m[M_RHS], d + kWxE + kWyE, i0 - 2, j0 - 1, q, &barB[s]);
+      tma_plane(&maps.m[M_INVD], d + kWxE + kWyE + kRhsE, i0 - 2, j0 - 1, q, &barB[s]);
+      ++issuedB;
+    };
+    auto waitA = [&](int q) {
+      const unsigned n = baseA + (unsigned)q;
+      return mbar_wait(&barA[n % kASlots], (n / kASlots) & 1u, kWaitPolls);
+    };
+    auto waitB = [&](int q) {
+      const unsigned n = baseB + (unsigned)q;
+      return mbar_wait(&barB[n % kBSlots], (n / kBSlots) & 1u, kWaitPolls);
+    };
+    if (tid == 0) {
+      for (int q = ka - 2; q <= ka + kDA - 4 && q <= lastA; ++q) issueA(q);
+      for (int q = ka - 1; q <= ka + kDB - 4 && q <= lastB; ++q) issueB(q);
+    }
+    // red role: the ring point's elements in the 12-row and 10-row boxes (column offset 0)
     const int rj = j0 - 1 + rr;
     const bool red_row_in = red_role && rj >= 2 && rj <= a.my;
-    const int e0 = (rr + 1) * kBX + (rx + 1);
+    const int e12 = (rr + 1) * kBX + (rx + 1), e10 = e12 - kBX;
     const int roff0 = par - rj - (i0 - 1) - rx;
-    auto red_value = [&](int q, int* xs) -> float {
-      const int off = (roff0 - q) & 1;
-      *xs = rx + off;
-      const int i = i0 - 1 + rx + off;
-      if (!(red_row_in && i >= 2 && i <= a.mx && q >= 2 && q <= a.mz)) return 0.f;
-      const int e = e0 + off;
-      const float* p1 = plane(q - 1);
-      const float* p2 = plane(q);
-      const float rh = p2[A_RHS * kSlotElems + e], inv = p2[A_INVD * kSlotElems + e];
-      if (zin) return (0.f - rh) * inv;
-      const float* p3 = plane(q + 1);
-      const float* ph = p2 + A_PHI * kSlotElems;
-      float s = p2[A_WZ * kSlotElems + e] * p3[A_PHI * kSlotElems + e];
-      s = fmaf(p1[A_WZ * kSlotElems + e], p1[A_PHI * kSlotElems + e], s);
-      s = fmaf(p2[A_WY * kSlotElems + e], ph[e + kBX], s);
-      s = fmaf(p2[A_WY * kSlotElems + e - kBX], ph[e - kBX], s);
-      s = fmaf(p2[A_WX * kSlotElems + e], ph[e + 1], s);
-      s = fmaf(p2[A_WX * kSlotElems + e - 1], ph[e - 1], s);
-      s = s - rh;
-      return s * inv;
-    };
-    // prologue: planes ka-2 .. ka+2 present, red(ka-1), red(ka), red(ka+1)
-    bool bad = false;
-    for (int q = ka - 2; q <= ka + 2; ++q) bad = bad || !wait(q);
-    if (__syncthreads_or(bad)) {
-      ok = false;
-      break;
-    }
-    if (red_role)
-      for (int q = ka - 1; q <= ka + 1; ++q) {
-        int x;
-        const float v = red_value(q, &x);
-        red[q & (kRedSlots - 1)][rr][x] = v;
-      }
-    __syncthreads();
+    // black role
     const int j = j0 + ty, ie = i0 + 2 * tx;
-    const int lr = ty + 1;                         // ring row of j
-    const int eb = (ty + 2) * kBX + (2 * tx + 2);  // box element of (ie, j)
+    const int lr = ty + 1;  // ring row of j
     const bool blk_row = blk_role && j <= a.my;
     const int boff0 = par - j - ie;
-    for (int k = ka; k < kb; ++k) {
-      if (tid == 0 && k + kAhead + 3 <= last_issue) {
-        // the copies of plane k+6 into the slot plane k-2 left (its last reader was step k-1)
-        const int q = k + kAhead + 3;
-        const unsigned sl = (base + (unsigned)q) & (kSlots - 1);
-        mbar_expect_tx(&bar[sl], bytes);
-        for (int arr = first; arr < kArrays; ++arr)
-          tma_plane(&maps.m[arr], ring + (sl * kArrays + arr) * kSlotElems, i0 - 2, j0 - 2, q, &bar[sl]);
-        ++issued;
+    // The black update's coefficients come through L2 (about a microsecond away): they are
+    // loaded one step ahead, into registers, so that their latency overlaps a whole step.
+    float cz = 0.f, czm = 0.f, cy = 0.f, cym = 0.f, cx = 0.f, cxm = 0.f, crh = 0.f, cinv = 0.f;
+    auto black_load = [&](int k) {
+      const int ib = ie + (((boff0 - k) & 1) ^ 1);
+      if (blk_row && k < kb && ib <= a.mx) {
+        const int pb = k * S + j * P + ib;
+        cz = __ldg(a.wz + pb), czm = __ldg(a.wz + pb - S);
+        cy = __ldg(a.wy + pb), cym = __ldg(a.wy + pb - P);
+        cx = __ldg(a.wx + pb), cxm = __ldg(a.wx + pb - 1);
+        crh = __ldg(a.rhs + pb), cinv = __ldg(a.invd + pb);
+      }
+    };
+    black_load(ka);
+    // Thread 0 alone waits for the copies, before the barrier that ends the previous step;
+    // the barrier then orders every other thread's reads after that completion. First the
+    // planes of step ka-3 (red(ka-1)): phi and wz of ka-2 .. ka, the group-B arrays of ka-1.
+    {
+      bool miss = false;
+      if (tid == 0) miss = !waitA(ka - 2) || !waitA(ka - 1) || !waitA(ka) || !waitB(ka - 1);
+      if (__syncthreads_or(miss)) {
+        ok = false;
+        break;
+      }
+    }
+    for (int k = ka - 3; k < kb; ++k) {
+      if (tid == 0) {
+        if (k + kDA <= lastA) issueA(k + kDA);
+        if (k + kDB <= lastB) issueB(k + kDB);
       }
       bool miss = false;
-      if (blk_row) {
-        // black(k) from red(k-1), red(k), red(k+1); both colours of plane k out. Plane k
-        // completed long ago (it is waited on here only to observe that completion).
-        miss = !wait(k);
+      if (blk_row && k >= ka) {
+        // black(k) from red(k-1), red(k), red(k+1); both colours of plane k out
         const float(*rm)[kRX] = red[(k - 1) & (kRedSlots - 1)];
         const float(*rc)[kRX] = red[k & (kRedSlots - 1)];
         const float(*rp)[kRX] = red[(k + 1) & (kRedSlots - 1)];
         const int roff = (boff0 - k) & 1;  // the red one of the pair: ie + roff
         const int xr = 2 * tx + 1 + roff, xb = 2 * tx + 1 + (roff ^ 1);
-        const long long prow = (long long)k * S + (long long)j * P;
+        const int prow = k * S + j * P;
         if (ie + roff <= a.mx) out[prow + ie + roff] = rc[lr][xr];
         const int ib = ie + (roff ^ 1);
-        if (ib <= a.mx && !miss) {
-          const int e = eb + (roff ^ 1);
-          const float* b0 = plane(k);
-          const float* bm = plane(k - 1);
-          float s = b0[A_WZ * kSlotElems + e] * rp[lr][xb];
-          s = fmaf(bm[A_WZ * kSlotElems + e], rm[lr][xb], s);
-          s = fmaf(b0[A_WY * kSlotElems + e], rc[lr + 1][xb], s);
-          s = fmaf(b0[A_WY * kSlotElems + e - kBX], rc[lr - 1][xb], s);
-          s = fmaf(b0[A_WX * kSlotElems + e], rc[lr][xb + 1], s);
-          s = fmaf(b0[A_WX * kSlotElems + e - 1], rc[lr][xb - 1], s);
-          s = s - b0[A_RHS * kSlotElems + e];
-          out[prow + ib] = s * b0[A_INVD * kSlotElems + e];
+        float v = 0.f;
+        if (ib <= a.mx) {
+          float s = cz * rp[lr][xb];
+          s = fmaf(czm, rm[lr][xb], s);
+          s = fmaf(cy, rc[lr + 1][xb], s);
+          s = fmaf(cym, rc[lr - 1][xb], s);
+          s = fmaf(cx, rc[lr][xb + 1], s);
+          s = fmaf(cxm, rc[lr][xb - 1], s);
+          s = s - crh;
+          v = s * cinv;
         }
-      } else if (red_role && k + 2 <= kb) {
-        // red(k+2) (needs plane k+3) into the red slot black(k-1) read last step
-        miss = !wait(k + 3);
-        if (!miss) {
-          int x;
-          const float v = red_value(k + 2, &x);
-          red[(k + 2) & (kRedSlots - 1)][rr][x] = v;
+        black_load(k + 1);
+        if (ib <= a.mx) out[prow + ib] = v;
+      }
+      if (red_role && k + 2 <= kb) {
+        // red(k+2): phi(k+1 .. k+3), wz(k+1 .. k+2) and the group-B arrays of plane k+2
+        {
+          const int q = k + 2;
+          const int off = (roff0 - q) & 1;
+          const int x = rx + off;
+          const int i = i0 - 1 + x;
+          float v = 0.f;
+          if (red_row_in && i >= 2 && i <= a.mx && q >= 2 && q <= a.mz) {
+            const float* A1 = sA + slotA(q - 1) * kAE;
+            const float* A2 = sA + slotA(q) * kAE;
+            const float* A3 = sA + slotA(q + 1) * kAE;
+            const float* B2 = sB + slotB(q) * kBE;
+            const int e = e12 + off, f = e10 + off;
+            const float rh = B2[kWxE + kWyE + f], inv = B2[kWxE + kWyE + kRhsE + f];
+            if (zin) {
+              v = (0.f - rh) * inv;
+            } else {
+              float s = A2[kPhiE + f] * A3[e];
+              s = fmaf(A1[kPhiE + f], A1[e], s);
+              s = fmaf(B2[kWxE + e], A2[e + kBX], s);
+              s = fmaf(B2[kWxE + e - kBX], A2[e - kBX], s);
+              s = fmaf(B2[f], A2[e + 1], s);
+              s = fmaf(B2[f - 1], A2[e - 1], s);
+              s = s - rh;
+              v = s * inv;
+            }
+          }
+          red[q & (kRedSlots - 1)][rr][x] = v;
         }
       }
+      // the next step's planes: phi and wz of k+4, the group-B arrays of k+3
+      if (tid == 0 && k + 3 <= kb) miss = !waitA(k + 4) || !waitB(k + 3);
       if (__syncthreads_or(miss)) {
         ok = false;
         break;
@@ -231,10 +280,15 @@ __global__ void __launch_bounds__(kThreads, 1)
       out[e] = __int_as_float(0x7fc00000);
     if (tid == 0) {
       atomicExch(&g_tma_fault, 1);
-      for (int s = 0; s < kSlots; ++s)
-        if (issued > (unsigned)s) {  // the last plane issued into slot s
-          const unsigned last = issued - 1 - ((issued - 1 - (unsigned)s) & (kSlots - 1));
-          mbar_wait(&bar[s], (last >> 3) & 1u, kWaitPolls);
+      for (int s = 0; s < kASlots; ++s)
+        if (issuedA > (unsigned)s) {  // the last copy issued into slot s
+          const unsigned last = issuedA - 1 - ((issuedA - 1 - (unsigned)s) % kASlots);
+          mbar_wait(&barA[s], (last / kASlots) & 1u, kWaitPolls);
+        }
+      for (int s = 0; s < kBSlots; ++s)
+        if (issuedB > (unsigned)s) {
+          const unsigned last = issuedB - 1 - ((issuedB - 1 - (unsigned)s) % kBSlots);
+          mbar_wait(&barB[s], (last / kBSlots) & 1u, kWaitPolls);
         }
     }
   }
@@ -252,13 +306,13 @@ PFN_cuTensorMapEncodeTiled_v12000 encoder() {
   return fn;
 }
 
-// a level array (padded extents, pitched) as a 3D FP32 tensor with 68 x 12 x 1 boxes
-bool level_map(CUtensorMap* m, const float* base, const Lvl<float>& a) {
+// a level array (padded extents, pitched) as a 3D FP32 tensor with 68 x rows x 1 boxes
+bool level_map(CUtensorMap* m, const float* base, const Lvl<float>& a, int rows) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = encoder();
   if (!enc) return false;
   const cuuint64_t dims[3] = {(cuuint64_t)a.mx + 3, (cuuint64_t)a.my + 3, (cuuint64_t)a.mz + 3};
   const cuuint64_t strides[2] = {(cuuint64_t)a.P * 4, (cuuint64_t)a.S * 4};
-  const cuuint32_t box[3] = {(cuuint32_t)kBX, (cuuint32_t)kBY, 1};
+  const cuuint32_t box[3] = {(cuuint32_t)kBX, (cuuint32_t)rows, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
   return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -299,11 +353,11 @@ int sweep_tma3d_fault() {
   return v;
 }
 
-// JMG_SWEEP3D=tma selects this kernel for the one-pass FP32 3D sweeps (read per launch,
-// i.e. when a solve's graph is captured); k_sweep_fused3d stays the default
+// the one-pass FP32 3D sweeps run here unless JMG_SWEEP3D=regs selects k_sweep_fused3d
+// (read per launch, i.e. when a solve's graph is captured)
 bool sweep_tma3d_enabled() {
   const char* e = getenv("JMG_SWEEP3D");
-  return e && std::strcmp(e, "tma") == 0;
+  return !(e && std::strcmp(e, "regs") == 0);
 }
 
 bool launch_sweep_tma3d(Lvl<float>& a, bool zero_in, cudaStream_t s) {
@@ -311,14 +365,14 @@ bool launch_sweep_tma3d(Lvl<float>& a, bool zero_in, cudaStream_t s) {
   // the six tensor maps of a level view, encoded once and kept (a few levels and both phi
   // buffers of a solve; the host work stays out of timed loops)
   struct Entry {
-    const float* src[kArrays];
+    const float* src[kMaps];
     int mx, my, mz, P;
     Maps maps;
   };
   static std::mutex mu;
   static Entry cache[16];
   static int ncache = 0, next = 0;
-  const float* src[kArrays] = {a.phi, a.rhs, a.wx, a.wy, a.wz, a.invd};
+  const float* src[kMaps] = {a.phi, a.wz, a.wx, a.wy, a.rhs, a.invd};
   Maps maps;
   {
     std::lock_guard<std::mutex> lock(mu);
@@ -332,8 +386,8 @@ bool launch_sweep_tma3d(Lvl<float>& a, bool zero_in, cudaStream_t s) {
       std::memset(&e, 0, sizeof(e));
       std::memcpy(e.src, src, sizeof(src));
       e.mx = a.mx, e.my = a.my, e.mz = a.mz, e.P = a.P;
-      for (int k = 0; k < kArrays; ++k)
-        if (!level_map(&e.maps.m[k], src[k], a)) return false;
+      for (int k = 0; k < kMaps; ++k)
+        if (!level_map(&e.maps.m[k], src[k], a, kRows[k])) return false;
       hit = ncache < 16 ? ncache++ : next;
       if (hit == next) next = (next + 1) % 16;
       cache[hit] = e;
@@ -341,13 +395,16 @@ bool launch_sweep_tma3d(Lvl<float>& a, bool zero_in, cudaStream_t s) {
     maps = cache[hit].maps;
   }
   // Neighbouring tiles must march up z together, so that the halo rows one block loads
-  // are still in L2 when the next block loads them: every block takes whole plane columns
-  // (chunks of one when there are fewer tiles than SMs). Ranges balanced over the SMs
-  // without regard to z read 2.1x the algorithmic bytes from DRAM (ncu: L2 hit rate 17 %).
+  // are still in L2 when the next block loads them: every block takes an equal share of
+  // one tile's plane column, as many shares per column as fill the resident blocks.
+  // Ranges balanced over the blocks without regard to z read 2.1x the algorithmic bytes
+  // from DRAM (ncu: L2 hit rate 17 %).
   const long long tiles = (long long)((a.mx - 1 + kTX - 1) / kTX) * ((a.my - 1 + kTY - 1) / kTY);
   const int planes = a.mz - 1;
   const long long total = tiles * planes;
-  const long long nchunk = tiles < num_sms() ? num_sms() / tiles : 1;
+  const long long resident = (long long)num_sms() * kBlocksPerSM;
+  long long nchunk = tiles < resident ? resident / tiles : 1;
+  if (nchunk > planes) nchunk = planes;
   const int per_block = (int)((planes + nchunk - 1) / nchunk);
   const int blocks = (int)((total + per_block - 1) / per_block);
   launch_k(k_sweep_tma3d, dim3((unsigned)blocks), dim3(kThreads), kSmem, s, maps, a, a.phi2, zero_in ? 1 : 0,

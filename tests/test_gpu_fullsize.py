@@ -31,7 +31,8 @@ from oracle import c_oracle, mg2d, mg3d  # noqa: E402
 
 TUNING = ("JMG_HOST_LOOP", "JMG_PDL", "JMG_COARSE_POINTS", "JMG_COARSE", "JMG_COARSE32", "JMG_FUSED", "JMG_FUSED2D",
           "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_RESTRICT3D", "JMG_PROLONG3D", "JMG_PROLONG2D", "JMG_FCG_BLOCKS",
-          "JMG_ADJ_BLOCK_POINTS", "JMG_COARSE_OPS", "JMG_FUSEDOPS", "JMG_FUSEDOPS_MAX", "JMG_COARSE_THREADS")
+          "JMG_ADJ_BLOCK_POINTS", "JMG_COARSE_OPS", "JMG_FUSEDOPS", "JMG_FUSEDOPS_MAX", "JMG_COARSE_THREADS",
+          "JMG_COARSE_WARP", "JMG_MID", "JMG_MID_POINTS", "JMG_MID_STALL", "JMG_SWEEP3D")
 
 
 def rel_l2(a, b):
@@ -98,13 +99,13 @@ def test_3d_256_onepass_fp32_sweep_bit_identical(p3d, monkeypatch):
 
 
 def test_3d_256_tma_sweep_equals_register_sweep(p3d, monkeypatch):
-    """The same mixed solve with the level-0 one-pass sweep fed by register loads (the
-    default) and by TMA copies (JMG_SWEEP3D=tma): the same bits."""
+    """The same mixed solve with the level-0 one-pass sweep fed by TMA copies (the default)
+    and by register loads (JMG_SWEEP3D=regs): the same bits."""
     grids, args, _ = p3d
     kw = dict(precision="mixed", fixed=True, max_iters_outer=3, fcycle=True)
     monkeypatch.setattr(_engine, "CACHE", _engine._Cache())
     phi_a, _ = solve_3d(*grids, *args, **kw)
-    monkeypatch.setenv("JMG_SWEEP3D", "tma")
+    monkeypatch.setenv("JMG_SWEEP3D", "regs")
     monkeypatch.setattr(_engine, "CACHE", _engine._Cache())
     phi_b, _ = solve_3d(*grids, *args, **kw)
     np.testing.assert_array_equal(phi_a, phi_b)

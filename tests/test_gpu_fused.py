@@ -77,14 +77,14 @@ def test_one_pass_equals_colour_passes(monkeypatch, shape, opts):
     ((128, 128, 64), dict(precision="mixed", stop="residual", outer="fcg", inner_cycles=2, fcycle=True))])
 def test_tma_sweep_equals_register_sweep(monkeypatch, shape, opts):
     """FP32 one-pass sweeps with their plane tiles fed by TMA copies (mg_sweep_tma3d.cu,
-    JMG_SWEEP3D=tma) and by register loads (k_sweep_fused3d, the default), on every level
+    the default) and by register loads (k_sweep_fused3d, JMG_SWEEP3D=regs), on every level
     of at least 4096 points: the same bits. On these small levels the blocks' work ranges
     cut the tiles' plane columns at arbitrary planes, so the march's restart at a tile
     boundary is covered too."""
     grids = tuple(grid_1D(m) for m in shape)
     args = _problem(*shape, seed=3 + sum(shape))
-    ref, c_ref = _solve(monkeypatch, {"JMG_FUSED_POINTS": "4096"}, grids, args, **opts)
-    got, c_got = _solve(monkeypatch, {"JMG_FUSED_POINTS": "4096", "JMG_SWEEP3D": "tma"}, grids, args, **opts)
+    ref, c_ref = _solve(monkeypatch, {"JMG_FUSED_POINTS": "4096", "JMG_SWEEP3D": "regs"}, grids, args, **opts)
+    got, c_got = _solve(monkeypatch, {"JMG_FUSED_POINTS": "4096"}, grids, args, **opts)
     assert int(c_got) == int(c_ref)
     assert torch.equal(got, ref)
 
