@@ -15,7 +15,8 @@ LIB = os.path.join(HERE, "libjmg.so")
 SOURCES = ["mg_kernels.cu", "mg_hierarchy.cu", "mg_aux.cu", "mg_driver.cu", "mg_noalloc.cu", "mg_coarse.cu", "mg_tile2d.cu",
            "mg_adjoint_kernels.cu", "mg_adjoint.cu", "mg_net.cu", "mg_krylov.cu", "mg_tangent.cu",
            "mg_batch.cu", "mg_fused.cu", "mg_tile3d.cu", "mg_fusedops2d.cu", "mg_coarse_staged.cu",
-           "mg_mid2d.cu", "mg_sweep_tma3d.cu"]
+           "mg_mid2d.cu", "mg_sweep_tma3d.cu",
+           "mg_fusedops3d.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 

@@ -133,21 +133,29 @@ int validate_and_layout(JmgPlan* p) {
   const bool fused64 = fused_on && fe64 && fe64[0] == '1';
   const char* fe2 = getenv("JMG_FUSED2D");
   const bool fused2d = fe2 && fe2[0] == '1';
-  // fused operator pairs (mg_fusedops2d.cu) on the 2D levels the grid-wide kernels run
-  // (more points than the single-block coarse kernel takes), 5-point stencil;
-  // JMG_FUSEDOPS=0 turns them off
+  // fused operator pairs on the levels the grid-wide kernels run (more points than the
+  // single-block coarse kernel takes): 2D (mg_fusedops2d.cu, 5-point stencil) by default,
+  // JMG_FUSEDOPS=0 turns them off; 3D (mg_fusedops3d.cu) only with JMG_FUSEDOPS3D=1, since
+  // they measured no faster there (3D 256^3 mixed + FCG 95.2 against 94.8 ms, plain FP64
+  // 1316 against 1280 ms: within a graph the small levels' launches already overlap, and
+  // the halos add FP64 work)
   const char* fo = getenv("JMG_FUSEDOPS");
-  const bool fuseops_on = d == 2 && !p->off_diag && !(fo && fo[0] == '0');
+  const char* fo3 = getenv("JMG_FUSEDOPS3D");
+  const bool fuseops_on =
+      !p->off_diag && !(fo && fo[0] == '0') && (d == 2 || (fo3 && fo3[0] == '1'));
   const long long block_limit = coarse_block_points();
   // Largest fused level (padded points): every FP32 level, FP64 levels up to 2^19 points.
   // On larger FP64 levels the halos' extra FP64 work outweighs the saved launches (2D
   // 1024^2 plain FP64, measured: 40.7 ms with the 512^2 level and below fused, 43.5 ms
   // with level 0 too, 42.0 ms unfused; mixed + FCG 6.97 ms all fused, 7.73 ms unfused).
   // JMG_FUSEDOPS_MAX overrides it.
+  // 3D: levels up to 2^19 padded points (64^3 and smaller), where launches are bound by
+  // latency; on larger ones the halos' recomputation (about 3.5 sweeps' work per owned
+  // point) outweighs the saved launches. JMG_FUSEDOPS_MAX overrides both.
   const long long fuse_max = [&] {
     const char* e = getenv("JMG_FUSEDOPS_MAX");
     const long long v = e ? atoll(e) : 0;
-    return v > 0 ? v : (p->mixed ? (1LL << 62) : (1LL << 19));
+    return v > 0 ? v : ((p->mixed && d == 2) ? (1LL << 62) : (1LL << 19));
   }();
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -357,6 +365,7 @@ int jmg::coarse_setup(JmgPlan* p) {
     if (b <= 200 * 1024 && prepare_coarse_smem32(b) == 0) p->coarse_smem32 = b;
   }
   prepare_fused_ops2d();  // kernel attributes, set outside any stream capture
+  prepare_fused_ops3d();
   if (p->dim == 3 && p->mixed) sweep_tma3d_ready();
   mid_setup(p);
   cudaGetLastError();  // a refused attribute or occupancy query leaves no sticky error
@@ -526,8 +535,8 @@ void emit_cycle(const JmgPlan* p, LvlTable<T>& tab, const LvlTable<T>* dtab, con
     for (int k = 0; k < cp.nu1 - (fuse ? 1 : 0); ++k) sweep(k == 0);
   if (count) *count += 1;
   else if (fuse)
-    launch_smooth_restrict2d<T>(tab.l[lev], tab.l[lev + 1],
-                                cp.nu1 == 1 && ((top && top->zero_first) || zero_phi), s);
+    launch_smooth_restrict<T>(dim, tab.l[lev], tab.l[lev + 1], cp.nu1 == 1 && ((top && top->zero_first) || zero_phi),
+                              s);
   else launch_restrict<T>(dim, tab.l[lev], tab.l[lev + 1], s);
   bool first = true;  // phi of level lev + 1 is zero until its first visit
   if (fcycle)
@@ -540,7 +549,7 @@ void emit_cycle(const JmgPlan* p, LvlTable<T>& tab, const LvlTable<T>* dtab, con
     first = false;
   }
   if (count) *count += 1;
-  else if (fuse) launch_prolong_smooth2d<T>(tab.l[lev], tab.l[lev + 1], s);
+  else if (fuse) launch_prolong_smooth<T>(dim, tab.l[lev], tab.l[lev + 1], s);
   else launch_prolong<T>(dim, tab.l[lev], tab.l[lev + 1], cp.diag, s);
   for (int k = 0; k < cp.nu2 - (fuse ? 1 : 0); ++k) sweep(false);
 }
@@ -1265,14 +1274,14 @@ int jmg_op_smooth_restrict_ws(JmgPlan* p, int level, int fp32, void* ws, size_t 
   if (fused && (rc = coarse_setup(p))) return rc;  // the fused kernels' attributes
   if (fp32) {
     Lvl<float> f = lvl32(p, ws, level), c = lvl32(p, ws, level + 1);
-    if (fused) launch_smooth_restrict2d<float>(f, c, false, s);
+    if (fused) launch_smooth_restrict<float>(p->dim, f, c, false, s);
     else {
       launch_sweep<float>(p->dim, f, s);
       launch_restrict<float>(p->dim, f, c, s);
     }
   } else {
     Lvl<double> f = lvl64(p, ws, level), c = lvl64(p, ws, level + 1);
-    if (fused) launch_smooth_restrict2d<double>(f, c, false, s);
+    if (fused) launch_smooth_restrict<double>(p->dim, f, c, false, s);
     else {
       launch_sweep<double>(p->dim, f, s);
       launch_restrict<double>(p->dim, f, c, s);

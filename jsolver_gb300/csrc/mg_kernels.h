@@ -74,6 +74,20 @@ int fused_wave_permille(int mx, int my, int mz);
 template <typename T> void launch_smooth_restrict2d(Lvl<T>& f, const Lvl<T>& c, bool zero_in, cudaStream_t s);
 template <typename T> void launch_prolong_smooth2d(Lvl<T>& f, const Lvl<T>& c, cudaStream_t s);
 void prepare_fused_ops2d();
+// mg_fusedops3d.cu: the same pairs on 3D levels (7-point stencil)
+template <typename T> void launch_smooth_restrict3d(Lvl<T>& f, const Lvl<T>& c, bool zero_in, cudaStream_t s);
+template <typename T> void launch_prolong_smooth3d(Lvl<T>& f, const Lvl<T>& c, cudaStream_t s);
+void prepare_fused_ops3d();
+template <typename T>
+inline void launch_smooth_restrict(int dim, Lvl<T>& f, const Lvl<T>& c, bool zero_in, cudaStream_t s) {
+  if (dim == 3) launch_smooth_restrict3d<T>(f, c, zero_in, s);
+  else launch_smooth_restrict2d<T>(f, c, zero_in, s);
+}
+template <typename T>
+inline void launch_prolong_smooth(int dim, Lvl<T>& f, const Lvl<T>& c, cudaStream_t s) {
+  if (dim == 3) launch_prolong_smooth3d<T>(f, c, s);
+  else launch_prolong_smooth2d<T>(f, c, s);
+}
 // mg_tile2d.cu: defect + restriction with every fine defect computed once
 template <typename T> void launch_restrict_tile2d(const Lvl<T>& f, const Lvl<T>& c, cudaStream_t s);
 // mg_tile2d.cu: r32 = float(rhs - L_h phi) (FP64 arithmetic) on the interior, and per-block

@@ -23,7 +23,7 @@ struct LevelInfo {
   size_t phi2, phi2_32;   // second phi buffers (FP64, FP32) of levels swept in one pass or by
                           // the fused operator pairs; 0 if absent
   bool onepass64, onepass32;  // sweeps in one pass (FP64, FP32 arrays)
-  bool fuse_ops;              // 2D grid-wide level: fused smooth + restrict, prolong + smooth
+  bool fuse_ops;              // grid-wide level: fused smooth + restrict, prolong + smooth
 };
 
 }  // namespace jmg

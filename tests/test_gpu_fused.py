@@ -216,3 +216,40 @@ def test_fused_operator_pairs_2d_equal_unfused(monkeypatch, shape, opts):
     got, c_got = run({})
     assert int(c_got) == int(c_ref)
     assert torch.equal(got, ref)
+
+
+CASES_OPS_3D = [
+    ((64, 64, 64), dict(precision="mixed", stop="residual", outer="fcg", inner_cycles=2, fcycle=True)),
+    ((128, 128, 128), dict(precision="mixed", stop="residual", outer="fcg", inner_cycles=2, fcycle=True)),
+    ((64, 64, 64), dict(stop="residual", outer="fcg")),
+    ((64, 32, 128), dict(precision="mixed", fixed=True, max_iters_outer=5, gamma=2)),
+    ((64, 64, 64), dict(fixed=True, max_iters_outer=4, nu1=2, nu2=1)),
+    ((64, 64, 64), dict(precision="mixed", fixed=True, max_iters_outer=4, nu1=1, nu2=3)),
+    ((64, 64, 64), dict(fixed=True, max_iters_outer=3, nu1=2, nu2=0)),
+    ((64, 64, 64), dict(fixed=True, max_iters_outer=4, skip_pre=True, fcycle=True)),
+    ((32, 64, 64), dict(fixed=True, max_iters_outer=3, fcycle=True, gamma=2)),
+    ((64, 64, 64), dict()),
+]
+
+
+@pytest.mark.parametrize("shape,opts", CASES_OPS_3D, ids=lambda x: str(x))
+def test_fused_operator_pairs_3d_equal_unfused(monkeypatch, shape, opts):
+    """3D solves with the fused pairs on the levels of at most 2^19 points (smooth +
+    restrict, prolong + smooth over tiles with halos; JMG_FUSEDOPS3D=1) and with the
+    separate colour passes, tiled restriction and cell prolongation (the default): the same
+    bits and counts, in FP64 and FP32 cycles, every cycle shape and sweep count."""
+    grids = tuple(grid_1D(m) for m in shape)
+    args = _problem(*shape, seed=11 + sum(shape))
+
+    def run(env):
+        monkeypatch.delenv("JMG_FUSEDOPS3D", raising=False)
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        _engine.CACHE.plans.clear()
+        _engine.CACHE.ws.clear()
+        return solve_3d(*grids, *args, **opts)
+
+    ref, c_ref = run({})
+    got, c_got = run({"JMG_FUSEDOPS3D": "1"})
+    assert int(c_got) == int(c_ref)
+    assert torch.equal(got, ref)
