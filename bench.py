@@ -23,9 +23,9 @@ flushed (256 MB write) before every timed solve. ``e2e`` is the same solve throu
 public API (solve_2d / solve_3d on CUDA tensors) with the host->device copies of the
 inputs from pinned memory and the device->host copy of phi and the count inside the
 timed region. ``roofline`` is the kernel with the largest share of the solve in the
-committed launch list (profiles/launch_shares.json), timed alone with CUDA events;
-``roofline_fine`` the fine-level kernel beside it (the fused smooth + restrict launch where level 0
-runs the fused pairs, else the sweep). ``cpu_baseline`` is the median
+committed launch list (profiles/launch_shares.json) among those bench.py times alone with
+CUDA events: the level-0 sweep, the level-0 fused smooth + restrict (2D), the coarse block
+and the FCG step's FP64 residual; ``roofline_others`` holds the rest. ``cpu_baseline`` is the median
 time of full solves of the C oracle on all host cores. ``--gpus N`` under torchrun runs
 N independent replicas (the path does not shard).
 
@@ -75,6 +75,10 @@ def parse():
                          "auto: fcg for the mixed and learned forms, richardson for fp64")
     ap.add_argument("--workload", default="2d", choices=sorted(WORKLOADS))
     ap.add_argument("--cycle", default=None, choices=["V", "W", "F"])
+    ap.add_argument("--nu1", type=int, default=None,
+                    help="pre-smoothing sweeps of the timed form (reference: 1; mixed + FCG default: 1)")
+    ap.add_argument("--nu2", type=int, default=None,
+                    help="post-smoothing sweeps of the timed form (reference: 1; mixed + FCG default: 3)")
     ap.add_argument("--m", type=int, default=None)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -93,10 +97,17 @@ def parse():
         a.form = "mixed"
     if a.outer == "auto":
         a.outer = "richardson" if a.form == "fp64" else "fcg"
+    # The mixed + FCG form's cycle: one cycle per FCG step with nu1 = 1, nu2 = 3, the
+    # fastest of a measured sweep (2D 1024^2 V: 5.85 ms against 6.25 with two (1, 1) cycles
+    # per step, 6.08 with (3, 3) or (1, 2), 5.93 with (2, 3); 3D 256^3 F: 81.1 ms against
+    # 94.8, the same as (2, 2) and (3, 3)). Every other form keeps the reference's (1, 1).
+    fcg_mixed = a.outer == "fcg" and a.form in ("mixed", "learned-mixed")
     if a.inner_cycles is None:
-        # two V-cycles per FCG step amortise the step's FP64 vector work (2D 1024^2:
-        # 9.1 vs 9.4 ms; 3D 256^3 F-cycles: even)
-        a.inner_cycles = 2 if a.outer == "fcg" and a.form in ("mixed", "learned-mixed") else 1
+        a.inner_cycles = 1
+    if a.nu1 is None:
+        a.nu1 = 1
+    if a.nu2 is None:
+        a.nu2 = 3 if fcg_mixed else 1
     return a
 
 
@@ -377,7 +388,7 @@ def batch_bench(args):
     X = [torch.from_numpy(np.stack([p[k] for p in probs])).to(dev) for k in keys]
     precision = "mixed" if args.form in ("mixed", "learned-mixed") else "fp64"
     opts = dict(stop="residual", rtol=RTOL, precision=precision, max_iters_outer=20000, outer=args.outer,
-                **cycle_kw(args.cycle))
+                nu1=args.nu1, nu2=args.nu2, **cycle_kw(args.cycle))
     if precision == "mixed":
         opts["inner_cycles"] = args.inner_cycles
     flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device=dev)
@@ -409,6 +420,7 @@ def batch_bench(args):
             "data": "synthetic (seeded GRF coefficients, manufactured rhs)",
             "config": {"workload": f"batch of {nb} 2d-{m}^2-random-coeff, {args.cycle}-cycles, "
                                    f"{precision}, outer {args.outer}", "lanes": args.lanes,
+                       "nu1": args.nu1, "nu2": args.nu2, "inner_cycles": args.inner_cycles,
                        "l2": "flushed (256 MB write) before every step"},
             "ms_per_batch": t_b, "sequential_ms": t_s, "sequential_solves_per_s": nb / (t_s / 1e3),
             "speedup_vs_sequential": t_s / t_b, "cycles_mean": float(cnt_b.double().mean()),
@@ -462,7 +474,7 @@ def timed_alone(fn, stream, flush, n):
 
 def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, dev, learned_cmp_on=True):
     """One workload's line: the form's solve (value, e2e), the plain FP64 comparison, the
-    roofline of the dominant kernel and of the fine sweep, and the CPU baseline."""
+    roofline of the dominant kernel and of the other timed kernels, and the CPU baseline."""
     import torch
     import torch.distributed as dist
     from jsolver_gb300 import _engine, _lib, workloads
@@ -477,7 +489,8 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
     kw = cycle_kw(cycle)
     learned = args.form.startswith("learned") and dim == 2
     precision = "mixed" if args.form in ("mixed", "learned-mixed") else "fp64"
-    opts = dict(stop="residual", rtol=RTOL, precision=precision, max_iters_outer=20000, outer=args.outer, **kw)
+    opts = dict(stop="residual", rtol=RTOL, precision=precision, max_iters_outer=20000, outer=args.outer,
+                nu1=args.nu1, nu2=args.nu2, **kw)
     if precision == "mixed":
         opts["inner_cycles"] = args.inner_cycles
     lib = _lib.load()
@@ -544,7 +557,7 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
         if not args.no_compare and (args.form != "fp64" or args.outer != "richardson"):
             # the plain FP64 multigrid from phi0 = 0 on the same problem, timed the same way
             plan64 = _lib.Plan(grid, _engine.make_config(**dict(opts, precision="fp64", inner_cycles=1,
-                                                                outer="richardson")))
+                                                                outer="richardson", nu1=1, nu2=1)))
             ws64 = torch.empty(plan64.workspace_bytes, dtype=torch.uint8, device=dev)
             f64 = lambda s: solve_dev(s, plan64, ws64, False)  # noqa: E731
             ms64 = timed(f64, plain_steps, max(3, min(warmup, 3)))
@@ -611,6 +624,8 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
                       "peak": peak, "unit": "GB/s", "peak_source": peak_src,
                       "alg_bytes_per_launch": alg_sweep / launches_per_sweep,
                       "launch_ms": sweep_ms / launches_per_sweep, "traffic": traffic}
+        roof_sweep["frac"] = roof_sweep["achieved"] / peak
+        cands = {"sweep": roof_sweep}
         if dim == 2 and lib.jmg_plan_level_fused(plan.handle, 0, fp32):
             # level 0 runs the fused pairs: time its smooth + restrict launch (reads phi, rhs,
             # the two face arrays, 1/A_cc and A_cc; writes phi's second buffer and the coarse
@@ -620,13 +635,29 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
             sr(stream)
             sr_ms = timed_alone(sr, stream, flush, 20)
             alg_sr = (7 * n0 + 2 * (m // 2 + 3) ** 2) * elem
-            roof_sweep = {"bound": "hbm", "kernel": f"k_smooth_restrict2d<{'float' if fp32 else 'double'}> (level 0: "
-                                                     "last pre-sweep + defect + restriction, one launch)",
-                          "achieved": alg_sr / (sr_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-                          "peak_source": peak_src, "alg_bytes_per_launch": alg_sr, "launch_ms": sr_ms,
-                          "traffic": load_json("profiles/traffic.json").get(
-                              f"smooth_restrict_{'fp32' if fp32 else 'fp64'}_2d_{m}")}
-        roof_sweep["frac"] = roof_sweep["achieved"] / peak
+            cands["smooth_restrict"] = {
+                "bound": "hbm", "kernel": f"k_smooth_restrict2d<{'float' if fp32 else 'double'}> (level 0: "
+                                          "last pre-sweep + defect + restriction, one launch)",
+                "achieved": alg_sr / (sr_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s", "peak_source": peak_src,
+                "alg_bytes_per_launch": alg_sr, "launch_ms": sr_ms,
+                "traffic": load_json("profiles/traffic.json").get(f"smooth_restrict_{'fp32' if fp32 else 'fp64'}_2d_{m}")}
+        if args.outer == "fcg" and precision == "mixed":
+            # the exact FP64 residual that ends every FCG step: reads x, rhs, the d face
+            # arrays and A_cc (FP64), writes the FP32 residual: ((d + 3) * 8 + 4) * N0 bytes;
+            # its d + 4 FP64 operations per point make it FP64-issue-bound as much as
+            # bandwidth-bound on GB300
+            fr = lambda s_: _lib.check(lib.jmg_op_fcg_residual_ws(plan.handle, *wsa, vp(s_.cuda_stream)))  # noqa: E731
+            fr(stream)
+            fr_ms = timed_alone(fr, stream, flush, 20)
+            alg_fr = ((dim + 3) * 8 + 4) * n0
+            cands["fcg_residual"] = {
+                "bound": "hbm", "kernel": f"k_fcg32_init<{dim}> (FP64 residual of the FCG step, FP32 copy, "
+                                          "partial norms; one launch)",
+                "achieved": alg_fr / (fr_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s", "peak_source": peak_src,
+                "alg_bytes_per_launch": alg_fr, "launch_ms": fr_ms,
+                "traffic": load_json("profiles/traffic.json").get(f"fcg_residual_{dim}d_{m}")}
+        for v in cands.values():
+            v["frac"] = v["achieved"] / peak
         # the coarse sub-cycle (one launch from the first coarse level down)
         lib.jmg_op_coarse_ws(plan.handle, fp32, *wsa, vp(stream.cuda_stream))
         cstart = lib.jmg_plan_coarse_start(plan.handle)
@@ -644,6 +675,7 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
                        "traffic": load_json("profiles/traffic.json").get(
                            f"coarse_{'fp32' if fp32 else 'fp64'}_{dim}d_{m}")}
         roof_coarse["frac"] = roof_coarse["achieved"] / peak
+        cands["coarse"] = roof_coarse
 
         # end to end through the public API from pinned host buffers
         host = {k: torch.from_numpy(p[k]).pin_memory() for k in ["phi0", "rhs", "lam"] + cn}
@@ -681,13 +713,14 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
     lib.jmg_plan_launch_counts(plan.handle, ctypes.byref(fixed_n), ctypes.byref(per_cycle))
     launches = steps * (fixed_n.value + per_cycle.value * cycles + (GUESS_LAUNCHES if learned else 0))
 
-    # the kernel with the largest share of the solve in the committed launch list
-    shares = load_json("profiles/launch_shares.json").get(f"{dim}d_{m}_{args.form}_{args.outer}_{cycle}", {})
-    dominant = "coarse" if shares.get("coarse", 0.0) > shares.get("fine", 0.0) else "fine"
-    roof = dict(roof_coarse if dominant == "coarse" else roof_sweep)
-    roof["launch_share"] = shares.get(dominant)
-    roof_other = dict(roof_sweep if dominant == "coarse" else roof_coarse)
-    roof_other["launch_share"] = shares.get("fine" if dominant == "coarse" else "coarse")
+    # the kernel with the largest share of the solve in the committed launch list (shares
+    # per candidate: the level-0 sweep, the level-0 smooth + restrict, the coarse block, the
+    # FCG residual); the others beside it
+    shares = load_json("profiles/launch_shares.json").get(
+        f"{dim}d_{m}_{args.form}_{args.outer}_{cycle}_nu{args.nu1}{args.nu2}_x{args.inner_cycles}", {})
+    dominant = max(cands, key=lambda k: shares.get(k, 0.0))
+    roof = dict(cands[dominant], launch_share=shares.get(dominant))
+    roof_others = {k: dict(v, launch_share=shares.get(k)) for k, v in cands.items() if k != dominant}
 
     line = {
         "metric": metric_name(dim, m), "value": ms, "unit": "ms", "n_gpus": ws_n, "steps": steps,
@@ -699,6 +732,7 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
                    "form": args.form, "stop": f"rel. residual <= {RTOL}",
                    "cycles": cycles * (args.inner_cycles if precision == "mixed" else 1),
                    "inner_cycles": args.inner_cycles if precision == "mixed" else None, "outer": args.outer,
+                   "nu1": args.nu1, "nu2": args.nu2,
                    "l2": "flushed (256 MB write) before every timed solve", "parallelism": f"replicas x{ws_n}"},
         "solves_per_s": 1e3 / ms * ws_n,
         "final_rel_residual": rel_res,
@@ -708,7 +742,7 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
         "learned_guess_form": learned_cmp,
         "max_err_vs_exact_discrete": err_exact,
         "roofline": roof,
-        "roofline_fine" if dominant == "coarse" else "roofline_coarse": roof_other,
+        "roofline_others": roof_others,
         "e2e": ({"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
                 if e2e_ms is not None else None),
         "gpu_launches": int(launches),

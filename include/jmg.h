@@ -243,6 +243,12 @@ int jmg_op_smooth32_ws(JmgPlan* plan, int level, int nsweeps, void* workspace, s
  * branch of multigrid_cycle (solver_2d.py:582-614) without copies, for timing it alone.
  * fp32 != 0: the FP32 arrays of a mixed-precision plan. */
 int jmg_op_coarse_ws(JmgPlan* plan, int fp32, void* workspace, size_t workspace_bytes, jmg_stream_t stream);
+/* The exact FP64 residual that ends every step of a mixed-precision FCG solve alone
+ * (rho = rhs - L_h x on level 0, its FP32 copy for the next cycle, the partial sums of
+ * rho . rho), on the arrays already in the workspace, for timing it; the plan needs
+ * JMG_OUTER_FCG and JMG_PREC_MIXED. No reference counterpart: the reference's stopping
+ * test is a distance, and it has no Krylov outer iteration. */
+int jmg_op_fcg_residual_ws(JmgPlan* plan, void* workspace, size_t workspace_bytes, jmg_stream_t stream);
 /* First level the coarse sub-cycle takes (valid after the plan's first solve or
  * jmg_op_coarse_ws on a GPU; before that the single-block rule's choice). No reference
  * counterpart. */

@@ -67,6 +67,7 @@ _SIGS = {
     "jmg_op_smooth_ws": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_size_t, _P]),
     "jmg_op_smooth32_ws": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_size_t, _P]),
     "jmg_op_coarse_ws": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t, _P]),
+    "jmg_op_fcg_residual_ws": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "jmg_plan_coarse_start": (ctypes.c_int, [_P]),
     "jmg_plan_mid_start": (ctypes.c_int, [_P]),
     "jmg_plan_level_fused": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),

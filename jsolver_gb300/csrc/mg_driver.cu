@@ -1256,6 +1256,19 @@ int jmg_op_coarse_ws(JmgPlan* p, int fp32, void* ws, size_t bytes, jmg_stream_t 
   return JMG_OK;
 }
 
+int jmg_op_fcg_residual_ws(JmgPlan* p, void* ws, size_t bytes, jmg_stream_t stream) {
+  int rc = check_ws(p, ws, bytes);
+  if (rc) return rc;
+  if (!p->fcg || !p->mixed)
+    return set_err(JMG_ERR_VALUE, "jmg_op_fcg_residual_ws needs a plan with outer fcg and precision mixed");
+  // the kernel that ends every mixed FCG step (launch_fcg32_iter): rho = rhs - L x in FP64,
+  // r32 = float(rho), partial sums of rho . rho
+  launch_fcg32_init(p->dim, lvl64(p, ws, 0), lvl32(p, ws, 0).rhs, nullptr, nullptr,
+                    ptr<double>(ws, p->off_fcg_parts) + 4 * fcg_num_parts(), (cudaStream_t)stream);
+  JMG_CUDA(cudaGetLastError());
+  return JMG_OK;
+}
+
 int jmg_plan_coarse_start(const JmgPlan* p) { return p ? p->coarse_start : -1; }
 int jmg_plan_mid_start(const JmgPlan* p) { return p && p->mid_start >= 0 && p->mid_now ? p->mid_start : -1; }
 
