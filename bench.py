@@ -78,7 +78,8 @@ def parse():
     ap.add_argument("--nu1", type=int, default=None,
                     help="pre-smoothing sweeps of the timed form (reference: 1; mixed + FCG default: 1)")
     ap.add_argument("--nu2", type=int, default=None,
-                    help="post-smoothing sweeps of the timed form (reference: 1; mixed + FCG default: 3)")
+                    help="post-smoothing sweeps of the timed form (reference: 1; mixed + FCG default: 5 in 2D, "
+                         "3 in 3D)")
     ap.add_argument("--m", type=int, default=None)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -97,18 +98,21 @@ def parse():
         a.form = "mixed"
     if a.outer == "auto":
         a.outer = "richardson" if a.form == "fp64" else "fcg"
-    # The mixed + FCG form's cycle: one cycle per FCG step with nu1 = 1, nu2 = 3, the
-    # fastest of a measured sweep (2D 1024^2 V: 5.85 ms against 6.25 with two (1, 1) cycles
-    # per step, 6.08 with (3, 3) or (1, 2), 5.93 with (2, 3); 3D 256^3 F: 81.1 ms against
-    # 94.8, the same as (2, 2) and (3, 3)). Every other form keeps the reference's (1, 1).
-    fcg_mixed = a.outer == "fcg" and a.form in ("mixed", "learned-mixed")
     if a.inner_cycles is None:
         a.inner_cycles = 1
-    if a.nu1 is None:
-        a.nu1 = 1
-    if a.nu2 is None:
-        a.nu2 = 3 if fcg_mixed else 1
     return a
+
+
+def form_nu(args, dim):
+    """(nu1, nu2) of the timed form. The mixed + FCG form runs one cycle per FCG step with
+    nu1 = 1 and nu2 = 5 in 2D, 3 in 3D: the fastest of a measured sweep (2D 1024^2 V:
+    5.75 ms, against 5.79 with (1, 4), 5.88 with (1, 3), 6.25 with two (1, 1) cycles per
+    step; 3D 256^3 F: 81.1 ms with (1, 3), (2, 2) or (2, 4), 81.6 with (1, 4), 94.8 with two
+    (1, 1) cycles). Every other form keeps the reference's (1, 1); --nu1 / --nu2 override."""
+    fcg_mixed = args.outer == "fcg" and args.form in ("mixed", "learned-mixed")
+    nu1 = args.nu1 if args.nu1 is not None else 1
+    nu2 = args.nu2 if args.nu2 is not None else ((5 if dim == 2 else 3) if fcg_mixed else 1)
+    return nu1, nu2
 
 
 # kernel launches of one learned guess: input pooling, RMS, packing (3); 12 convolutions,
@@ -388,7 +392,7 @@ def batch_bench(args):
     X = [torch.from_numpy(np.stack([p[k] for p in probs])).to(dev) for k in keys]
     precision = "mixed" if args.form in ("mixed", "learned-mixed") else "fp64"
     opts = dict(stop="residual", rtol=RTOL, precision=precision, max_iters_outer=20000, outer=args.outer,
-                nu1=args.nu1, nu2=args.nu2, **cycle_kw(args.cycle))
+                nu1=form_nu(args, 2)[0], nu2=form_nu(args, 2)[1], **cycle_kw(args.cycle))
     if precision == "mixed":
         opts["inner_cycles"] = args.inner_cycles
     flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device=dev)
@@ -420,7 +424,7 @@ def batch_bench(args):
             "data": "synthetic (seeded GRF coefficients, manufactured rhs)",
             "config": {"workload": f"batch of {nb} 2d-{m}^2-random-coeff, {args.cycle}-cycles, "
                                    f"{precision}, outer {args.outer}", "lanes": args.lanes,
-                       "nu1": args.nu1, "nu2": args.nu2, "inner_cycles": args.inner_cycles,
+                       "nu1": form_nu(args, 2)[0], "nu2": form_nu(args, 2)[1], "inner_cycles": args.inner_cycles,
                        "l2": "flushed (256 MB write) before every step"},
             "ms_per_batch": t_b, "sequential_ms": t_s, "sequential_solves_per_s": nb / (t_s / 1e3),
             "speedup_vs_sequential": t_s / t_b, "cycles_mean": float(cnt_b.double().mean()),
@@ -489,8 +493,9 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
     kw = cycle_kw(cycle)
     learned = args.form.startswith("learned") and dim == 2
     precision = "mixed" if args.form in ("mixed", "learned-mixed") else "fp64"
+    nu1, nu2 = form_nu(args, dim)
     opts = dict(stop="residual", rtol=RTOL, precision=precision, max_iters_outer=20000, outer=args.outer,
-                nu1=args.nu1, nu2=args.nu2, **kw)
+                nu1=nu1, nu2=nu2, **kw)
     if precision == "mixed":
         opts["inner_cycles"] = args.inner_cycles
     lib = _lib.load()
@@ -717,7 +722,7 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
     # per candidate: the level-0 sweep, the level-0 smooth + restrict, the coarse block, the
     # FCG residual); the others beside it
     shares = load_json("profiles/launch_shares.json").get(
-        f"{dim}d_{m}_{args.form}_{args.outer}_{cycle}_nu{args.nu1}{args.nu2}_x{args.inner_cycles}", {})
+        f"{dim}d_{m}_{args.form}_{args.outer}_{cycle}_nu{nu1}{nu2}_x{args.inner_cycles}", {})
     dominant = max(cands, key=lambda k: shares.get(k, 0.0))
     roof = dict(cands[dominant], launch_share=shares.get(dominant))
     roof_others = {k: dict(v, launch_share=shares.get(k)) for k, v in cands.items() if k != dominant}
@@ -732,7 +737,7 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
                    "form": args.form, "stop": f"rel. residual <= {RTOL}",
                    "cycles": cycles * (args.inner_cycles if precision == "mixed" else 1),
                    "inner_cycles": args.inner_cycles if precision == "mixed" else None, "outer": args.outer,
-                   "nu1": args.nu1, "nu2": args.nu2,
+                   "nu1": nu1, "nu2": nu2,
                    "l2": "flushed (256 MB write) before every timed solve", "parallelism": f"replicas x{ws_n}"},
         "solves_per_s": 1e3 / ms * ws_n,
         "final_rel_residual": rel_res,
