@@ -115,12 +115,13 @@ int validate_and_layout(JmgPlan* p) {
   if (p->cfg.off_diag && d != 2) return set_err(JMG_ERR_VALUE, "off_diag (D_xy) is a 2D option");
   p->off_diag = d == 2 && p->cfg.off_diag;
   p->lv.resize(p->used);
-  // one-pass sweeps (mg_fused.cu), 5- and 7-point stencils: the 3D levels whose one-pass
-  // grid fills at least half a wave of the GPU (256^3 levels and finer); with
-  // JMG_FUSED2D=1 also the 2D levels of at least 2^18 padded points (512^2 and finer:
-  // faster alone from a cold L2, but not inside a 2D solve, where the level stays in L2);
-  // with JMG_FUSED_POINTS set, every level of at least that many padded points. These
-  // levels get a second phi buffer. FP32 levels by default, FP64 levels too with
+  // one-pass sweeps (mg_fused.cu, mg_sweep_tma3d.cu), 5- and 7-point stencils: the 3D
+  // levels whose one-pass grid fills at least half a wave of the GPU (256^3 levels and
+  // finer) and the 2D grid-wide levels (more points than the coarse block takes; they
+  // run the sweeps beyond the fused pairs' two, e.g. the four extra post-sweeps of a
+  // V(1,5) cycle: 2D 1024^2 mixed + FCG 5.65 against 5.79 ms; JMG_FUSED2D=0 turns the 2D
+  // ones off); with JMG_FUSED_POINTS set, every level of at least that many padded points.
+  // These levels get a second phi buffer. FP32 levels by default, FP64 levels too with
   // JMG_FUSED64=1; JMG_FUSED=0 turns them off.
   const long long fused_min = [] {
     const char* e = getenv("JMG_FUSED_POINTS");
@@ -132,7 +133,7 @@ int validate_and_layout(JmgPlan* p) {
   const bool fused_on = !p->off_diag && !(fe && fe[0] == '0');
   const bool fused64 = fused_on && fe64 && fe64[0] == '1';
   const char* fe2 = getenv("JMG_FUSED2D");
-  const bool fused2d = fe2 && fe2[0] == '1';
+  const bool fused2d = !(fe2 && fe2[0] == '0');
   // fused operator pairs on the levels the grid-wide kernels run (more points than the
   // single-block coarse kernel takes): 2D (mg_fusedops2d.cu, 5-point stencil) by default,
   // JMG_FUSEDOPS=0 turns them off; 3D (mg_fusedops3d.cu) only with JMG_FUSEDOPS3D=1, since
@@ -188,7 +189,7 @@ int validate_and_layout(JmgPlan* p) {
         fused_on && li.elems < (1ULL << 31) &&  // the one-pass kernels index with 32 bits
         (fused_min > 0 ? (long long)li.elems >= fused_min
                        : d == 3 ? fused_wave_permille(li.m[0], li.m[1], li.m[2]) >= 500
-                                : fused2d && (long long)li.elems >= (1LL << 18));
+                                : fused2d && (long long)li.box.nx * li.box.ny > block_limit);
     li.onepass64 = fused_level && fused64;
     li.onepass32 = fused_level && p->mixed;
     const long long pts = (long long)li.box.nx * li.box.ny * li.box.nz;
@@ -278,7 +279,9 @@ static void mid_setup(JmgPlan* p) {
     bool fused = true;
     for (int k = l; k < p->coarse_start; ++k) {
       const LevelInfo& lk = p->lv[k];
-      fused = fused && lk.fuse_ops && (p->mixed ? lk.phi2_32 && !lk.onepass32 : lk.phi2 && !lk.onepass64);
+      // (the kernel runs a level's sweeps beyond the fused pairs as its own colour passes,
+      // whatever the level's one-pass flag: the same bits)
+      fused = fused && lk.fuse_ops && (p->mixed ? lk.phi2_32 != 0 : lk.phi2 != 0);
     }
     if (!fused) continue;
     MidOps ops;

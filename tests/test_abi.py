@@ -94,6 +94,7 @@ def test_fused_operator_pairs_cut_launches(monkeypatch):
     prolongation): every FP32 level, FP64 levels up to 2^19 padded points."""
     lib = _lib.load()
     g = _engine.make_grid((grid_1D(1024), grid_1D(1024)))
+    monkeypatch.setenv("JMG_FUSED2D", "0")  # colour passes wherever a level sweeps on its own
 
     def per_cycle(env, **kw):
         monkeypatch.delenv("JMG_FUSEDOPS", raising=False)
@@ -115,9 +116,9 @@ def test_fused_operator_pairs_cut_launches(monkeypatch):
 
 def test_sweep_launches_per_level(monkeypatch):
     """One-pass sweeps: 3D levels whose one-pass grid fills half a wave (256^3 and finer),
-    2D levels of at least 2^18 padded points with JMG_FUSED2D=1, FP32 by default, FP64
-    with JMG_FUSED64=1, none with JMG_FUSED=0 or with D_xy; each has a second phi buffer.
-    JMG_FUSED_POINTS selects levels by size instead."""
+    the 2D grid-wide levels (more padded points than the coarse block takes; off with
+    JMG_FUSED2D=0), FP32 by default, FP64 with JMG_FUSED64=1, none with JMG_FUSED=0 or with
+    D_xy; each has a second phi buffer. JMG_FUSED_POINTS selects levels by size instead."""
     lib = _lib.load()
     for k in ("JMG_FUSED", "JMG_FUSED64", "JMG_FUSED_POINTS", "JMG_FUSED2D"):
         monkeypatch.delenv(k, raising=False)
@@ -140,9 +141,10 @@ def test_sweep_launches_per_level(monkeypatch):
     assert [lib.jmg_plan_sweep_launches(small.handle, lv, 1) for lv in range(3)] == [1, 2, 2]
     monkeypatch.delenv("JMG_FUSED_POINTS")
     g2 = _engine.make_grid((grid_1D(1024),) * 2)
-    assert [lib.jmg_plan_sweep_launches(_lib.Plan(g2, mixed).handle, lv, 1) for lv in range(3)] == [2, 2, 2]
-    monkeypatch.setenv("JMG_FUSED2D", "1")
     p2 = _lib.Plan(g2, mixed)
-    # 2D opt-in: 1027 x 1040 and 515 x 528 padded points sweep in one pass, 259 x 272 in two
-    assert [lib.jmg_plan_sweep_launches(p2.handle, lv, 1) for lv in range(3)] == [1, 1, 2]
+    # 2D: the grid-wide levels 1024^2 .. 64^2 sweep in one pass, the coarse block's levels
+    # (35^2 = 1225 padded points and fewer) in colour passes
+    assert [lib.jmg_plan_sweep_launches(p2.handle, lv, 1) for lv in range(7)] == [1, 1, 1, 1, 1, 2, 2]
+    monkeypatch.setenv("JMG_FUSED2D", "0")
+    assert [lib.jmg_plan_sweep_launches(_lib.Plan(g2, mixed).handle, lv, 1) for lv in range(3)] == [2, 2, 2]
     assert lib.jmg_plan_sweep_launches(_lib.Plan(g2, _engine.make_config(off_diag=True)).handle, 0, 0) == 4
