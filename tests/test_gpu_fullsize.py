@@ -111,9 +111,13 @@ def test_3d_256_tma_sweep_equals_register_sweep(p3d, monkeypatch):
     np.testing.assert_array_equal(phi_a, phi_b)
 
 
-def test_2d_1024_headline_form_reaches_rtol(p2d):
+@pytest.mark.parametrize("form", [dict(inner_cycles=2), dict(nu2=5, inner_cycles=1)], ids=["V11x2", "V15x1"])
+def test_2d_1024_headline_form_reaches_rtol(p2d, form):
+    """The mixed + FCG form with two V(1,1) cycles per step and with one V(1,5) cycle per
+    step (bench.py's fast form; its extra post-sweeps run as one-pass launches): the
+    oracle's FP64 residual meets the tolerance."""
     grids, args, p = p2d
-    phi, c = solve_2d(*grids, *args, stop="residual", rtol=1e-10, precision="mixed", outer="fcg", inner_cycles=2)
+    phi, c = solve_2d(*grids, *args, stop="residual", rtol=1e-10, precision="mixed", outer="fcg", **form)
     o = mg2d.Oracle2D(*grids)
     o.setup(*args)
     assert o.rel_residual(phi, p["rhs"]) <= 2e-10
@@ -121,10 +125,12 @@ def test_2d_1024_headline_form_reaches_rtol(p2d):
     assert int(c) < 60
 
 
-def test_3d_256_headline_form_reaches_rtol(p3d):
+@pytest.mark.parametrize("form", [dict(inner_cycles=2), dict(nu2=3, inner_cycles=1)], ids=["F11x2", "F13x1"])
+def test_3d_256_headline_form_reaches_rtol(p3d, form):
+    """The same for 3D F-cycles: two F(1,1) or one F(1,3) cycle per FCG step."""
     grids, args, p = p3d
-    phi, c = solve_3d(*grids, *args, stop="residual", rtol=1e-10, precision="mixed", outer="fcg", inner_cycles=2,
-                      fcycle=True)
+    phi, c = solve_3d(*grids, *args, stop="residual", rtol=1e-10, precision="mixed", outer="fcg", fcycle=True,
+                      **form)
     o = mg3d.Oracle3D(*grids)
     o.setup(*args)
     assert o.rel_residual(phi, p["rhs"]) <= 2e-10
