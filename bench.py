@@ -141,19 +141,71 @@ def dist_env():
 
 
 class Clocks:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    """SM clock and clock-event reasons of the GPU, sampled during the timed region.
+
+    NVML is read from a background thread every 5 ms (the timed regions last tens of
+    milliseconds); where the NVML library cannot be loaded, nvidia-smi samples every 100 ms.
+    Only read-only queries are made: no setting of the GPU is touched. The GPU is found by
+    its UUID, so a remapped CUDA_VISIBLE_DEVICES still names the right one."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    POLL_S = 0.005
+    NVML_CLOCK_SM = 1
+    # nvmlClocksEventReason* bit masks of nvml.h
+    REASON_BITS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+                   0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
 
-    def __init__(self, index):
-        self.index = index
-        self.p = None
+    def __init__(self, index, uuid=None):
+        self.index, self.uuid = index, uuid
+        self.p = self.nvml = self.thread = None
+        self.sm, self.smax, self.reasons, self.out = [], None, set(), ""
+
+    def _nvml_open(self):
+        nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            return False
+        h = ctypes.c_void_p()
+        rc = (nv.nvmlDeviceGetHandleByUUID(f"GPU-{self.uuid}".encode(), ctypes.byref(h)) if self.uuid else 1)
+        if rc != 0 and nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.index), ctypes.byref(h)) != 0:
+            nv.nvmlShutdown()
+            return False
+        self.reasons_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        if nv.nvmlDeviceGetMaxClockInfo(h, self.NVML_CLOCK_SM, ctypes.byref(mx)) == 0:
+            self.smax = float(mx.value)
+        self.nvml, self.h = nv, h
+        return True
+
+    def _nvml_sample(self):
+        clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        if self.nvml.nvmlDeviceGetClockInfo(self.h, self.NVML_CLOCK_SM, ctypes.byref(clk)) == 0:
+            self.sm.append(float(clk.value))
+        if self.reasons_fn(self.h, ctypes.byref(rs)) == 0:
+            self.reasons.update(n for b, n in self.REASON_BITS.items() if rs.value & b)
+
+    def _nvml_loop(self):
+        while not self.stop.wait(self.POLL_S):
+            self._nvml_sample()
 
     def __enter__(self):
+        import threading
         try:
-            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+            ok = self._nvml_open()
+        except (OSError, AttributeError):
+            ok = False
+        if ok:
+            self._nvml_sample()  # one sample before the region starts, so the record is never empty
+            self.stop = threading.Event()
+            self.thread = threading.Thread(target=self._nvml_loop, daemon=True)
+            self.thread.start()
+            return self
+        self.nvml = None
+        try:
+            ident = f"GPU-{self.uuid}" if self.uuid else str(self.index)
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={ident}", f"--query-gpu={self.Q}",
                                        "--format=csv,noheader,nounits", "-lms", "100"],
                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
@@ -161,6 +213,10 @@ class Clocks:
         return self
 
     def __exit__(self, *a):
+        if self.thread is not None:
+            self.stop.set()
+            self.thread.join()
+            self.nvml.nvmlShutdown()
         if self.p is not None:
             self.p.terminate()
             try:
@@ -171,24 +227,37 @@ class Clocks:
         return False
 
     def summary(self):
-        if self.p is None:
+        if self.nvml is None and self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sm, smax, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in getattr(self, "out", "").splitlines():
-            f = [x.strip() for x in line.split(",")]
-            if len(f) < 9:
-                continue
-            try:
-                sm.append(float(f[1]))
-                smax = float(f[2])
-            except ValueError:
-                continue
-            for n, v in zip(names, f[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        if self.p is not None:
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for line in self.out.splitlines():
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    self.sm.append(float(f[1]))
+                    self.smax = float(f[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        self.reasons.add(n)
+        return {"sm_mhz": float(np.median(self.sm)) if self.sm else None, "sm_max_mhz": self.smax,
+                "min_sm_mhz": min(self.sm) if self.sm else None, "reasons": sorted(self.reasons),
+                "samples": len(self.sm), "source": "nvml" if self.nvml is not None else "nvidia-smi"}
+
+
+def gpu_uuid(dev):
+    """The CUDA device's UUID as hex digits and dashes (NVML and nvidia-smi take it with
+    a 'GPU-' prefix), or None where torch does not report one."""
+    import torch
+    try:
+        u = str(torch.cuda.get_device_properties(dev).uuid).strip()
+    except (AttributeError, RuntimeError):
+        return None
+    u = u[4:] if u.startswith("GPU-") else u
+    return u if u and all(c in "0123456789abcdefABCDEF-" for c in u) else None
 
 
 def cpu_full_solves(p, dim, m, kw, runs, budget_s):
@@ -569,7 +638,7 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
             plain = {"ms": ms64, "cycles": int(count.item()), "final_rel_residual": rel_residual(plan64, ws64),
                      "steps": plain_steps}
             del ws64
-        with Clocks(local) as clk:
+        with Clocks(local, gpu_uuid(dev)) as clk:
             ms = timed(solve_dev, steps, warmup)
         cycles = int(count.item())
         rel_res = rel_residual(plan, wsb)
