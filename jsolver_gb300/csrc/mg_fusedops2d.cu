@@ -15,8 +15,10 @@ __global__ void __launch_bounds__(NT) k_smooth_restrict2d(Lvl<T> f, T* __restric
   smooth_restrict_tile<T, CJ, CI, NT, false>(f, out, c, zero_in, blockIdx.y, blockIdx.x, smraw);
 }
 
+// FP32: held to 32 registers, so 4 blocks of 512 threads fit on an SM and the 512 tiles of
+// a 1024^2 level run in one wave (608 resident blocks; at 34 registers 3 fitted, 456)
 template <typename T, int TJ, int TI, int NT>
-__global__ void __launch_bounds__(NT) k_prolong_smooth2d(Lvl<T> f, T* __restrict__ out, Lvl<T> c) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 0) k_prolong_smooth2d(Lvl<T> f, T* __restrict__ out, Lvl<T> c) {
   pdl_enter();
   extern __shared__ __align__(16) unsigned char smraw[];
   prolong_smooth_tile<T, TJ, TI, NT, false>(f, out, c, blockIdx.y, blockIdx.x, smraw);
