@@ -757,29 +757,40 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
         phi_host = torch.empty(out.shape, dtype=torch.float64).pin_memory()
         cnt_host = torch.empty((), dtype=torch.int64).pin_memory()
 
-        def e2e_step():
+        def e2e_step(marks=None):
             for k in host:
                 dst[k].copy_(host[k], non_blocking=True)
+            if marks:
+                marks[0].record(stream)
             solve = solve_2d if dim == 2 else solve_3d
             extra = {"guess": net} if learned else {}
             phi, cnt = solve(*((g,) * dim), dst["phi0"], dst["rhs"], dst["lam"], *[dst[k] for k in cn], **opts,
                              **extra)
+            if marks:
+                marks[1].record(stream)
             phi_host.copy_(phi, non_blocking=True)
             cnt_host.copy_(cnt, non_blocking=True)
 
         for _ in range(0 if args.no_e2e else 2):
             e2e_step()
         stream.synchronize()
-        e2e_t = []
+        e2e_t, e2e_parts = [], []
         for _ in range(0 if args.no_e2e else steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            marks = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
             e0.record(stream)
-            e2e_step()
+            e2e_step(marks)
             e1.record(stream)
             e1.synchronize()
             e2e_t.append(e0.elapsed_time(e1))
+            e2e_parts.append((e0.elapsed_time(marks[0]), marks[0].elapsed_time(marks[1]), marks[1].elapsed_time(e1)))
         e2e_ms = float(np.mean(e2e_t)) if e2e_t else None
+        # mean device time of each part of the end-to-end step: the input copies, the
+        # solve call, the result copies
+        e2e_split = ({"h2d_ms": float(np.mean([t[0] for t in e2e_parts])),
+                      "solve_ms": float(np.mean([t[1] for t in e2e_parts])),
+                      "d2h_ms": float(np.mean([t[2] for t in e2e_parts]))} if e2e_parts else None)
         h2d = sum(t.numel() * 8 for t in host.values())
         d2h = phi_host.numel() * 8 + 8
 
@@ -817,8 +828,8 @@ def measure(args, dim, m, cycle, steps, warmup, plain_steps, ws_n, rank, local, 
         "max_err_vs_exact_discrete": err_exact,
         "roofline": roof,
         "roofline_others": roof_others,
-        "e2e": ({"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
-                if e2e_ms is not None else None),
+        "e2e": ({"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                 "split": e2e_split} if e2e_ms is not None else None),
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
