@@ -33,7 +33,7 @@ def grf(shape, spacing, corr_len, sigma, rng):
         sh[ax] = k.size
         k2 = k2 + (k.reshape(sh)) ** 2
     f *= np.exp(-0.25 * k2 * corr_len ** 2)  # sqrt of the Gaussian spectral density
-    g = np.fft.irfftn(f, s=shape)
+    g = np.fft.irfftn(f, s=shape, axes=tuple(range(len(shape))))
     g -= g.mean()
     g /= g.std()
     return sigma * g
