@@ -96,7 +96,8 @@ def p2d_11(xc, yc, shape):  # test_solver_2d.py:807-836
     Dyy = dpar * c2 + dperp * s2
     Dxy = (dperp - dpar) * sca
     r2 = x ** 2 + y ** 2
-    dpx, dpy = -y / r2, x / r2
+    with np.errstate(divide="ignore", invalid="ignore"):  # r2 = 0 at the origin, as defined
+        dpx, dpy = -y / r2, x / r2
     dDxx_dx = 2 * (dpar - dperp) * sca * dpx
     dDyy_dy = 2 * (dperp - dpar) * sca * dpy
     dDxy_dx = (dperp - dpar) * (c2 - s2) * dpx

@@ -43,7 +43,7 @@ def _gpu_grads(gx, gy, p, w, **opts):
     phi, _ = solve_2d(gx, gy, *[ts[k] for k in NAMES], fixed=True, **opts)
     loss = (phi * torch.tensor(w, device=DEV)).sum()
     loss.backward()
-    return float(loss), {k: ts[k].grad.cpu().numpy() for k in NAMES}
+    return float(loss.detach()), {k: ts[k].grad.cpu().numpy() for k in NAMES}
 
 
 def _ref_grads(gx, gy, p, w, iters, gamma=1, fcycle=False, nu1=1, nu2=1):
@@ -52,7 +52,7 @@ def _ref_grads(gx, gy, p, w, iters, gamma=1, fcycle=False, nu1=1, nu2=1):
     phi = t.solve_fixed(*[ts[k] for k in NAMES], iters=iters)
     loss = (phi * torch.tensor(w)).sum()
     loss.backward()
-    return float(loss), {k: ts[k].grad.numpy() for k in NAMES}
+    return float(loss.detach()), {k: ts[k].grad.numpy() for k in NAMES}
 
 
 def _rel(a, b):

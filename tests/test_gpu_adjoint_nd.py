@@ -63,7 +63,7 @@ def _gpu3(grids, p, w, **opts):
     phi, _ = solve_3d(*grids, *[ts[k] for k in NAMES3], fixed=True, **opts)
     loss = (phi * torch.tensor(w, device=DEV)).sum()
     loss.backward()
-    return float(loss), {k: ts[k].grad.cpu().numpy() for k in NAMES3}
+    return float(loss.detach()), {k: ts[k].grad.cpu().numpy() for k in NAMES3}
 
 
 def _gpu9(grids, p, w, **opts):
@@ -71,7 +71,7 @@ def _gpu9(grids, p, w, **opts):
     phi, _ = solve_2d(*grids, *[ts[k] for k in NAMES9[:5]], D_xy=ts["D_xy"], fixed=True, **opts)
     loss = (phi * torch.tensor(w, device=DEV)).sum()
     loss.backward()
-    return float(loss), {k: ts[k].grad.cpu().numpy() for k in NAMES9}
+    return float(loss.detach()), {k: ts[k].grad.cpu().numpy() for k in NAMES9}
 
 
 def _ref3(grids, p, w, iters, **form):
@@ -80,7 +80,7 @@ def _ref3(grids, p, w, iters, **form):
     phi = t.solve_fixed(*[ts[k] for k in NAMES3], iters=iters)
     loss = (phi * torch.tensor(w)).sum()
     loss.backward()
-    return float(loss), {k: ts[k].grad.numpy() for k in NAMES3}
+    return float(loss.detach()), {k: ts[k].grad.numpy() for k in NAMES3}
 
 
 def _ref9(grids, p, w, iters, **form):
@@ -89,7 +89,7 @@ def _ref9(grids, p, w, iters, **form):
     phi = t.solve_fixed(*[ts[k] for k in NAMES9[:5]], iters=iters, Dxy=ts["D_xy"])
     loss = (phi * torch.tensor(w)).sum()
     loss.backward()
-    return float(loss), {k: ts[k].grad.numpy() for k in NAMES9}
+    return float(loss.detach()), {k: ts[k].grad.numpy() for k in NAMES9}
 
 
 def _check(loss, g, rloss, rg, names):
